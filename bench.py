@@ -1,0 +1,363 @@
+"""Benchmark of the NCVis fit_transform hot path on GB300.
+
+Headline workload: fit_transform of N=1,024,000 x D=100 float32 unit vectors
+from a 128-component von Mises-Fisher mixture (kappa=50, Dirichlet(1)
+weights, seed 42), cosine distance, n_neighbors=15, d=2, 50 epochs, 20 init
+epochs, the reference's default noise plan and a/b (spread 1, min_dist 0.4).
+
+One step = one full fit_transform (preprocess, kNN, symmetrize, init, SGD)
+on inputs already resident in HBM (X is 410 MB, larger than the 129 MB L2, so
+no explicit flush is needed between steps).  `e2e` times the same call
+through the C ABI with pinned host buffers (the H2D copy of X and the D2H
+copy of Y inside the timed region).  With --gpus N > 1 (one rank per GPU
+under torchrun) every rank embeds its own replica: the path shards only in
+its kNN stage, so replicas are what scale here.
+
+--impl reference times the reference's algorithm on the host cores (the
+oracle port in oracle/, all threads) on a bounded sample of the same
+workload and extrapolates it to the full size; see `sample` in its line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FULL, D_FULL, K_NN, D_EMB, EPOCHS, INIT_EPOCHS = 1_024_000, 100, 15, 2, 50, 20
+SAMPLE_N = 65_536  # CPU-baseline sample of the same generator
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--knn", choices=["fp32", "bf16"], default=os.environ.get("NCVIS_BENCH_KNN", "fp32"))
+    p.add_argument("--n", type=int, default=N_FULL, help="points (default: the full workload)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-recall", action="store_true")
+    return p.parse_args()
+
+
+def workload(n):
+    from ncvis_gb300.synthetic import vmf_mixture
+    X, _ = vmf_mixture(n, D_FULL, n_comp=128, kappa=50.0, seed=42)
+    return X
+
+
+def config(n, knn):
+    return {
+        "workload": f"fit_transform N={n} D={D_FULL} vMF mixture (128 comps, kappa=50), cosine, "
+                    f"n_neighbors={K_NN}, d={D_EMB}, {EPOCHS} epochs, {INIT_EPOCHS} init epochs",
+        "knn": "exact FP32" if knn == "fp32" else "BF16 tcgen05 + exact FP32 rerank",
+        "noise_plan": "reference default (sum 262)",
+        "l2": "inputs larger than L2 (X 410 MB)",
+        "parallelism": "replicas (one independent embedding per GPU)",
+    }
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, path, index):
+        self.path, self.index, self.proc = path, index, None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        seen = sorted({n for _, _, flags in rows for n, f in zip(names, flags) if "Active" in f})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": seen, "samples": len(rows)}
+
+
+# --------------------------------------------------------- distributed glue
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(value: float, device=None) -> float:
+    """Maximum of `value` over all ranks (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(device=None):
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        if device is not None and str(device).startswith("cuda"):
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+# ------------------------------------------------------- CPU (reference) arm
+
+def cpu_sample_pipeline(threads, steps, warmup, log=print):
+    """The reference's algorithm (oracle port, all host threads) on a
+    SAMPLE_N-point sample of the workload: kNN once (brute force, reported,
+    not in the value), then per step symmetrize + build_edges + init +
+    optimize, extrapolated linearly to N_FULL (all four are O(E))."""
+    from oracle import oracle as O
+    from ncvis_gb300.api import default_noise_plan, find_ab_params
+    X = workload(SAMPLE_N)
+    a, b = find_ab_params(1.0, 0.4)
+    plan = default_noise_plan(EPOCHS).astype(np.uint64)
+    t = time.perf_counter()
+    Xp = O.preprocess(X, 2)
+    inds, dists = O.knn(Xp, 2, K_NN, use_f64=False, n_threads=threads)
+    t_knn = time.perf_counter() - t
+    times = []
+    for s in range(warmup + steps):
+        t0 = time.perf_counter()
+        rp, cols, _ = O.symmetrize(inds, dists, n_threads=threads)
+        src = O.edges_from_csr(rp)
+        Y = O.init_embedding(SAMPLE_N, D_EMB, src, cols, 42, INIT_EPOCHS, np.float32(1 / K_NN),
+                             threads)
+        O.optimize(Y, 0.0, src, cols, 42, plan, a, b, n_threads=threads)
+        dt = time.perf_counter() - t0
+        if s >= warmup:
+            times.append(dt)
+        log(f"cpu step {s}: {dt:.2f}s (E={src.size})")
+    per_step = statistics.median(times)
+    scale = N_FULL / SAMPLE_N
+    return {
+        "value": per_step * scale,
+        "unit": "s",
+        "cores": threads,
+        "kind": "port",
+        "sample": (f"{SAMPLE_N} points of the same vMF generator; symmetrize+build_edges+init+"
+                   f"optimize timed ({per_step:.2f}s median of {len(times)}) and scaled by "
+                   f"N_full/N_sample={scale:.2f} (O(E) stages); the reference's HNSW kNN is "
+                   f"unavailable (hnswlib absent) and excluded, so this is a lower bound of its "
+                   f"fit_transform time; brute-force FP32 kNN of the sample took {t_knn:.2f}s"),
+        "sample_step_s": per_step,
+        "knn_bruteforce_sample_s": t_knn,
+        "edges_sample": int(src.size),
+    }
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    res = cpu_sample_pipeline(threads, args.steps, args.warmup, log=lambda m: print(m, file=sys.stderr))
+    line = {
+        "impl": "reference", "metric": "fit_transform_seconds", "value": res["value"], "unit": "s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["value"] * 1000.0, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded vMF mixture)",
+        "config": config(N_FULL, "fp32"),
+        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": res["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def recall_at_15(X, inds, n_queries=2000, seed=0):
+    """recall@15 of the engine's kNN table against FP64 exact search (numpy
+    BLAS) for a query subsample, same row contract (k+1 nearest by
+    (distance, index), nearest dropped)."""
+    rng = np.random.default_rng(seed)
+    q = np.sort(rng.choice(X.shape[0], n_queries, replace=False))
+    Xd = X.astype(np.float64)
+    Xd /= np.linalg.norm(Xd, axis=1, keepdims=True)
+    hits = 0
+    for s in range(0, n_queries, 500):
+        qi = q[s:s + 500]
+        dist = 1.0 - Xd[qi] @ Xd.T
+        part = np.argpartition(dist, K_NN + 1, axis=1)[:, :K_NN + 2]
+        for r, i in enumerate(qi):
+            cand = part[r]
+            order = np.lexsort((cand, dist[r, cand]))[:K_NN + 1]
+            exact = cand[order][1:]
+            hits += len(np.intersect1d(exact, inds[i]))
+    return hits / (n_queries * K_NN)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300 import _lib, stages
+
+    n = args.n
+    X = workload(n)
+    Xd = torch.from_numpy(X).to(dev)
+    vis = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
+                      random_seed=42, distance="cosine", knn_precision=args.knn)
+    for _ in range(args.warmup):
+        vis.fit_transform(Xd)
+    torch.cuda.synchronize()
+
+    L = _lib.lib()
+    stage_list = []
+    clocks_path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv") \
+        if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/ncvis_clocks_{os.getpid()}.csv"
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(dev)
+    torch.cuda.synchronize()
+    launches0 = L.ncvis_kernel_launch_count()
+    with ClockSampler(clocks_path, local) as clk:
+        start.record()
+        for _ in range(args.steps):
+            vis.fit_transform(Xd)
+            stage_list.append(vis.stage_times())
+        stop.record()
+        torch.cuda.synchronize()
+    launches = L.ncvis_kernel_launch_count() - launches0
+    barrier(dev)
+    step_s = start.elapsed_time(stop) / 1000.0 / args.steps
+    step_s = max_over_ranks(step_s, dev)
+
+    # e2e through the C ABI with pinned host buffers.
+    Xh = torch.from_numpy(X).pin_memory()
+    Yh = torch.empty((n, D_EMB), dtype=torch.float32).pin_memory()
+    import ctypes as C
+    L.ncvis_fit_transform(vis._h, Xh.data_ptr(), n, D_FULL, Yh.data_ptr())  # warm host path
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rc = L.ncvis_fit_transform(vis._h, Xh.data_ptr(), n, D_FULL, Yh.data_ptr())
+        e2e_times.append(time.perf_counter() - t0)
+        _lib.check(rc, vis._h)
+    e2e_s = max_over_ranks(statistics.mean(e2e_times), dev)
+
+    if rank != 0:
+        return 0
+
+    knn_ms = statistics.mean(s["knn_ms"] for s in stage_list)
+    opt_ms = statistics.mean(s["optimize_ms"] for s in stage_list)
+    E = int(stage_list[-1]["n_edges"])
+    plan = vis.noise_plan.astype(np.int64)
+    pair_updates = E * int((plan + 1).sum())
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    flops = 2.0 * n * n * D_FULL
+    if args.knn == "bf16":
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "unit": "TFLOP/s",
+                "peak_source": "bf16_tflops_sustained of measured" if peaks else "fallback"}
+    else:
+        # No measured FP32-SIMT peak exists; nominal FFMA rate.
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        roof = {"bound": "fp32_simt", "unit": "TFLOP/s",
+                "peak_source": "nominal FP32 FFMA (152 SMs x 128 lanes x 2 flop x 2.07 GHz)"}
+    achieved = flops / (knn_ms / 1000.0) / 1e12
+    roof.update({"kernel": "knn candidate selection", "achieved": achieved, "peak": peak,
+                 "frac": achieved / peak, "traffic": None,
+                 "algorithmic": f"2*N^2*D = {flops:.3e} FLOP per launch (D=100 unpadded)"})
+    sgd_bytes = E * (EPOCHS * 4 + 16 * D_EMB * int((plan + 1).sum()))
+    sgd_gbs = sgd_bytes / (opt_ms / 1000.0) / 1e9
+    hbm = peaks.get("hbm_gbs", 6800.0)
+
+    recall = None
+    if not args.no_recall:
+        inds, _ = stages.knn(Xd, K_NN, 2, precision=1 if args.knn == "bf16" else 0)
+        recall = recall_at_15(X, inds.cpu().numpy())
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu_full = cpu_sample_pipeline(os.cpu_count() or 1, 1, 0, log=lambda m: print(m, file=sys.stderr))
+        cpu = {k: cpu_full[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    line = {
+        "metric": "fit_transform_seconds", "value": step_s, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1000.0,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.knn == "fp32" else "bf16+f32",
+        "data": "synthetic (seeded vMF mixture, no dataset)", "config": config(n, args.knn),
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": n * D_FULL * 4,
+                "d2h_bytes_per_step": n * D_EMB * 4},
+        "roofline": roof,
+        "sgd": {"pair_updates_per_s": pair_updates / (opt_ms / 1000.0),
+                "edge_epochs_per_s": E * EPOCHS / (opt_ms / 1000.0), "optimize_ms": opt_ms,
+                "algorithmic_GBps": sgd_gbs, "hbm_peak_GBps": hbm, "frac_of_hbm": sgd_gbs / hbm,
+                "E": E},
+        "recall_at_15": recall,
+        "stage_ms": {k: statistics.mean(s[k] for s in stage_list) for k in
+                     ("preprocess_ms", "knn_ms", "rerank_ms", "symmetrize_ms", "init_ms",
+                      "optimize_ms")},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

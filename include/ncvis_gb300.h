@@ -1,0 +1,186 @@
+/*
+ * ncvis_gb300.h — C ABI of the GB300 NCVis engine (libncvis_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every function returns an int status
+ * (NCVIS_OK == 0) unless stated otherwise; the message of the last failure is
+ * available from ncvis_last_error(handle) or, for the handle-less stage
+ * functions, ncvis_get_last_error() (per calling thread).
+ *
+ * Reference interfaces replaced (stat-ml/ncvis):
+ *   ncvis_params / ncvis_create  <- ncvis::NCVis::NCVis(...)   src/ncvis.hpp:54, src/ncvis.cpp:12-21
+ *   ncvis_destroy                <- ncvis::NCVis::~NCVis()      src/ncvis.hpp:55, src/ncvis.cpp:23-30
+ *   ncvis_fit_transform          <- ncvis::NCVis::fit_transform src/ncvis.hpp:66, src/ncvis.cpp:354-459
+ *   ncvis_distance               <- enum ncvis::Distance        src/ncvis.hpp:27-32
+ *   ncvis_knn_device             <- NCVis::buildKNN + findKNN   src/ncvis.cpp:72-153
+ *   ncvis_symmetrize_device      <- KNNTable::symmetrize + NCVis::build_edges
+ *                                   src/knntable.cpp:24-99, src/ncvis.cpp:155-173
+ *   ncvis_init_embedding_device  <- NCVis::init_embedding       src/ncvis.cpp:184-273
+ *   ncvis_optimize_device        <- NCVis::optimize             src/ncvis.cpp:275-352
+ *   ncvis_optimize_replay_device <- NCVis::optimize, one thread src/ncvis.cpp:275-352
+ * The C++ header include/ncvis.hpp wraps this ABI in a class with the
+ * reference's exact constructor and fit_transform signatures.
+ */
+#ifndef NCVIS_GB300_H
+#define NCVIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define NCVIS_OK 0
+#define NCVIS_INVALID_ARGUMENT 1
+#define NCVIS_CUDA_ERROR 2
+#define NCVIS_UNSUPPORTED 3
+#define NCVIS_DEVICE_TIMEOUT 4
+#define NCVIS_INTERNAL 5
+
+/* Same values and order as ncvis::Distance (src/ncvis.hpp:27-32). */
+typedef enum ncvis_distance {
+    NCVIS_SQUARED_L2 = 0,
+    NCVIS_INNER_PRODUCT = 1,
+    NCVIS_COSINE_SIMILARITY = 2,
+    NCVIS_CORRELATION = 3
+} ncvis_distance;
+
+/* kNN precision modes (ncvis_options.knn_precision). */
+#define NCVIS_KNN_FP32 0      /* exact FP32 distances: the plain drop-in form */
+#define NCVIS_KNN_BF16_RERANK 1 /* BF16 tensor-core distances, exact FP32 rerank */
+
+/* SGD modes (ncvis_options.sgd_mode). */
+#define NCVIS_SGD_HOGWILD 0 /* parallel chains, counter-based noise samples */
+#define NCVIS_SGD_REPLAY 1  /* one chain consuming a recorded noise stream */
+
+/* Constructor arguments of ncvis::NCVis (src/ncvis.hpp:54), same meaning.
+ * M and ef_construction configure HNSW in the reference and are accepted and
+ * ignored here (the kNN is exact).  n_threads bounds host-side work only.
+ * n_noise: n_epochs entries (copied at create), or NULL for 3 per epoch. */
+typedef struct ncvis_params {
+    size_t d;
+    size_t n_threads;
+    size_t n_neighbors;
+    size_t M;
+    size_t ef_construction;
+    size_t random_seed;
+    int n_epochs;
+    int n_init_epochs;
+    float a;
+    float b;
+    float alpha;
+    float alpha_Q;
+    const size_t *n_noise;
+    int distance; /* ncvis_distance */
+} ncvis_params;
+
+/* Engine options beyond the reference's constructor (all zero = defaults:
+ * FP32 exact kNN, Hogwild SGD, engine-owned stream, automatic chain count). */
+typedef struct ncvis_options {
+    int knn_precision;      /* NCVIS_KNN_FP32 | NCVIS_KNN_BF16_RERANK */
+    int rerank_factor;      /* candidates kept per point = rerank_factor * k (0: 2 for FP32, 4 for BF16) */
+    int sgd_mode;           /* NCVIS_SGD_HOGWILD | NCVIS_SGD_REPLAY */
+    const int32_t *replay_stream; /* host array of noise indices in one-thread draw order (replay) */
+    size_t replay_len;      /* entries in replay_stream: E * sum(n_noise) */
+    void *stream;           /* cudaStream_t to run on; NULL: the engine's own stream */
+    int sgd_chains;         /* parallel SGD chains; 0: automatic */
+} ncvis_options;
+
+/* Per-stage device times of the last fit_transform, in milliseconds, named
+ * after the reference's DEBUG stage timers (src/ncvis.cpp:370-437). */
+typedef struct ncvis_stage_times {
+    float h2d_ms;
+    float preprocess_ms;
+    float knn_ms;        /* candidate selection (buildKNN + findKNN) */
+    float rerank_ms;     /* exact rerank of the candidates */
+    float symmetrize_ms;
+    float build_edges_ms;
+    float init_ms;
+    float optimize_ms;
+    float d2h_ms;
+    float total_ms;
+    int64_t n_edges;     /* symmetrized directed edges E */
+    int64_t k;           /* neighbours per point after clamping */
+} ncvis_stage_times;
+
+typedef struct ncvis_engine *ncvis_handle;
+
+/* Engine lifetime.  ncvis_create returns NULL on invalid parameters (the
+ * reason is in ncvis_get_last_error()).  `options` may be NULL. */
+ncvis_handle ncvis_create(const ncvis_params *params, const ncvis_options *options);
+void ncvis_destroy(ncvis_handle h);
+int ncvis_set_options(ncvis_handle h, const ncvis_options *options);
+
+/* Host buffers: X [N, D] row-major float32 (read), Y [N, d] row-major float32
+ * (written).  Errors as the reference: N == 0 || D == 0, Y == NULL. */
+int ncvis_fit_transform(ncvis_handle h, const float *X, size_t N, size_t D, float *Y);
+
+/* Device buffers (same layout), enqueued on the engine's stream; returns
+ * after the work is enqueued and the edge count is known. */
+int ncvis_fit_transform_device(ncvis_handle h, const float *dX, size_t N, size_t D, float *dY);
+
+const char *ncvis_last_error(ncvis_handle h);
+const char *ncvis_get_last_error(void);
+int ncvis_get_stage_times(ncvis_handle h, ncvis_stage_times *out);
+
+/* ----------------------------------------------------------------------
+ * Stage-level entry points.  Device pointers, enqueued on `stream`
+ * (cudaStream_t, NULL = legacy default stream).  Indices are int32, so
+ * N < 2^31 and N * k < 2^30.
+ * -------------------------------------------------------------------- */
+
+/* Exact kNN table with the reference's row contract (src/ncvis.cpp:128-153):
+ * the k+1 smallest (distance, index) pairs of each preprocessed point over all
+ * points, the smallest dropped, the other k stored in descending order.
+ * Distances: squared L2, or 1 - <x, y> after the reference's preprocessing
+ * (centring for correlation, unit norm for cosine/correlation). */
+int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
+                     int rerank_factor, int32_t *d_inds, float *d_dists, void *stream);
+
+/* Symmetrization, bit-exact with the reference's one-thread
+ * KNNTable::symmetrize on the same table, emitted as CSR.  Rows are the
+ * reference's rows after sorting and deduplication; flattening them row by
+ * row gives NCVis::build_edges' edge list.  Capacity of d_cols / d_vals /
+ * d_src must be 2 * N * k.  d_src (optional, may be NULL) receives the source
+ * row of every entry.  *n_edges receives E (host). */
+int ncvis_symmetrize_device(size_t N, size_t k, const int32_t *d_inds, const float *d_dists,
+                            int64_t *d_row_ptr, int32_t *d_cols, float *d_vals, int32_t *d_src,
+                            size_t *n_edges, void *stream);
+
+/* init_embedding over a CSR graph: Y [N, d] ~ U(0,1) from the one-thread
+ * pcg64(seed) stream, then n_init_epochs of neighbour averaging with weight
+ * alpha followed by per-dimension standardisation. */
+int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
+                                const int32_t *d_cols, uint64_t seed, int n_init_epochs,
+                                float alpha, float *dY, void *stream);
+
+/* Parallel (Hogwild) NCE SGD over epochs [epoch_begin, epoch_end) of an
+ * n_epochs schedule; Y and *dQ (device float) updated in place.  n_noise:
+ * host array of n_epochs entries.  chains: 0 = automatic. */
+int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
+                          const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
+                          int epoch_begin, int epoch_end, int n_epochs, const size_t *n_noise,
+                          float a, float b, float alpha, float alpha_Q, int chains, void *stream);
+
+/* Replay: one chain runs edges [edge_begin, edge_end) of epoch `epoch` in
+ * order, reading noise samples from d_stream starting at stream_offset, with
+ * *dQ as the running normaliser copy (updated in place).  The arithmetic is
+ * the reference's one-thread optimizer's, sample by sample. */
+int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const int32_t *d_dst,
+                                 size_t edge_begin, size_t edge_end, const int32_t *d_stream,
+                                 size_t stream_offset, float *dY, float *dQ, int epoch,
+                                 int n_epochs, size_t n_noise_epoch, float a, float b, float alpha,
+                                 float alpha_Q, void *stream);
+
+/* Number of kernels this library has launched in the process so far. */
+uint64_t ncvis_kernel_launch_count(void);
+
+/* Library version string. */
+const char *ncvis_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCVIS_GB300_H */

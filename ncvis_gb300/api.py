@@ -1,0 +1,182 @@
+"""Python API of the GB300 NCVis engine, a drop-in for the reference's
+``ncvis.NCVis`` (wrapper/ncvis.pyx:48-163).
+
+The parameter policy is the reference's: the a/b curve fit
+(wrapper/ncvis.pyx:7-24, 137-141), the default noise schedule
+(wrapper/ncvis.pyx:103-123), the thread default (:125-126) and the distance
+names (:128-135), with the same ValueErrors.  ``fit_transform`` makes one call
+into libncvis_gb300.so, as the reference makes one call into its C++ engine
+(wrapper/ncvis.pyx:45-46, 159-163).  numpy input runs through the host-buffer
+entry point; a CUDA torch tensor runs through the device-buffer entry point
+on the current torch stream and returns a CUDA tensor.
+
+Keyword-only extras select the engine's modes: ``knn_precision`` ("fp32",
+the plain drop-in, or "bf16" for tensor-core distances with an exact FP32
+rerank), ``rerank_factor``, ``sgd_mode`` ("hogwild" or "replay" with a
+recorded ``replay_stream``) and ``sgd_chains``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from multiprocessing import cpu_count
+
+import numpy as np
+
+from . import _lib
+
+
+def find_ab_params(spread: float = 1.0, min_dist: float = 0.1):
+    """Fit a, b of the embedding kernel 1 / (1 + a x^(2b)) to an offset
+    exponential decay, as the reference does (wrapper/ncvis.pyx:7-24, after
+    UMAP's curve fit)."""
+    from scipy.optimize import curve_fit
+
+    def curve(x, a, b):
+        return 1.0 / (1.0 + a * x ** (2 * b))
+
+    xv = np.linspace(0, spread * 3, 300)
+    yv = np.zeros(xv.shape)
+    yv[xv < min_dist] = 1.0
+    yv[xv >= min_dist] = np.exp(-(xv[xv >= min_dist] - min_dist) / spread)
+    params, _ = curve_fit(curve, xv, yv)
+    return params[0], params[1]
+
+
+def default_noise_plan(n_epochs: int, n_negative: int = 5) -> np.ndarray:
+    """Noise samples per epoch rising as the cube of training progress and
+    summing to about n_epochs * n_negative, at least 1 (wrapper/ncvis.pyx:103-112)."""
+    plan = np.linspace(0, 1, n_epochs)
+    plan = plan ** 3
+    plan /= plan.sum()
+    plan *= n_epochs * n_negative
+    plan = plan.round().astype(np.uintp)
+    plan[plan < 1] = 1
+    return plan
+
+
+DISTANCES = {
+    "euclidean": 0,      # squared_L2
+    "cosine": 2,         # cosine_similarity
+    "correlation": 3,    # correlation
+    "inner_product": 1,  # inner_product
+}
+
+_PRECISIONS = {"fp32": _lib.KNN_FP32, "bf16": _lib.KNN_BF16_RERANK}
+_SGD_MODES = {"hogwild": _lib.SGD_HOGWILD, "replay": _lib.SGD_REPLAY}
+
+
+class NCVis:
+    def __init__(self, d=2, n_threads=-1, n_neighbors=15, M=8, ef_construction=100,
+                 random_seed=42, n_epochs=50, n_init_epochs=20, spread=1., min_dist=0.4, a=None,
+                 b=None, alpha=1., alpha_Q=1., n_noise=None, distance="euclidean", *,
+                 knn_precision="fp32", rerank_factor=0, sgd_mode="hogwild", replay_stream=None,
+                 sgd_chains=0):
+        """Creates a new NCVis instance; arguments as in the reference
+        (wrapper/ncvis.pyx:49-101).  M and ef_construction configure HNSW in
+        the reference and are accepted and ignored (the kNN here is exact);
+        n_threads bounds host-side work only."""
+        self.d = d
+        if n_noise is None:
+            negative_plan = default_noise_plan(n_epochs)
+        elif type(n_noise) is np.ndarray:
+            if len(n_noise.shape) != 1:
+                raise ValueError(
+                    "n_noise should have exactly one dimension, but shape {} was passed".format(
+                        n_noise.shape))
+            negative_plan = n_noise.astype(np.uintp)
+            n_epochs = negative_plan.size
+        elif type(n_noise) is int:
+            if n_noise < 1:
+                raise ValueError("n_noise should be at least 1, but {} was passed".format(n_noise))
+            negative_plan = np.full(n_epochs, n_noise).astype(np.uintp)
+        else:
+            raise ValueError("n_noise has unsupported type")
+
+        if n_threads < 1:
+            n_threads = cpu_count()
+
+        if distance not in DISTANCES:
+            raise ValueError("Unsupported distance, expected one of: "
+                             f"{set(DISTANCES)}, but got {distance}")
+
+        if (a is None) or (b is None):
+            if (a is None) and (b is None):
+                a, b = find_ab_params(spread, min_dist)
+            else:
+                raise ValueError("Expected (a, b) to be (float, float) or (None, None), "
+                                 f"but got (a, b) = ({a}, {b})")
+        if knn_precision not in _PRECISIONS:
+            raise ValueError(f"knn_precision must be one of {sorted(_PRECISIONS)}")
+        if sgd_mode not in _SGD_MODES:
+            raise ValueError(f"sgd_mode must be one of {sorted(_SGD_MODES)}")
+
+        self.n_epochs = int(n_epochs)
+        self.noise_plan = np.ascontiguousarray(negative_plan, dtype=np.uintp)
+        self.a, self.b = float(a), float(b)
+        self._noise_c = (C.c_size_t * max(1, self.n_epochs))(*[int(v) for v in self.noise_plan])
+        self._params = _lib.NcvisParams(
+            d=d, n_threads=n_threads, n_neighbors=n_neighbors, M=M,
+            ef_construction=ef_construction, random_seed=random_seed, n_epochs=self.n_epochs,
+            n_init_epochs=n_init_epochs, a=self.a, b=self.b, alpha=alpha, alpha_Q=alpha_Q,
+            n_noise=C.cast(self._noise_c, C.POINTER(C.c_size_t)), distance=DISTANCES[distance])
+        self._replay = None
+        if replay_stream is not None:
+            self._replay = np.ascontiguousarray(replay_stream, dtype=np.int32)
+        self._options = _lib.NcvisOptions(
+            knn_precision=_PRECISIONS[knn_precision], rerank_factor=int(rerank_factor),
+            sgd_mode=_SGD_MODES[sgd_mode],
+            replay_stream=(self._replay.ctypes.data_as(C.POINTER(C.c_int32))
+                           if self._replay is not None else None),
+            replay_len=0 if self._replay is None else int(self._replay.size),
+            stream=None, sgd_chains=int(sgd_chains))
+        L = _lib.lib()
+        self._h = L.ncvis_create(C.byref(self._params), C.byref(self._options))
+        if not self._h:
+            raise _lib.NcvisError(_lib.NCVIS_INVALID_ARGUMENT,
+                                  (L.ncvis_get_last_error() or b"").decode())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.lib().ncvis_destroy(h)
+            self._h = None
+
+    def _set_stream(self, stream_ptr):
+        self._options.stream = stream_ptr
+        _lib.check(_lib.lib().ncvis_set_options(self._h, C.byref(self._options)), self._h)
+
+    def fit_transform(self, X):
+        """Builds an embedding for the rows of X [n_samples, n_high_dimensions]
+        and returns Y [n_samples, d] float32 (wrapper/ncvis.pyx:145-163)."""
+        L = _lib.lib()
+        if _is_cuda_tensor(X):
+            import torch
+            Xc = X.detach().to(torch.float32).contiguous()
+            Y = torch.empty((Xc.shape[0], self.d), dtype=torch.float32, device=Xc.device)
+            with torch.cuda.device(Xc.device):
+                self._set_stream(torch.cuda.current_stream().cuda_stream)
+                rc = L.ncvis_fit_transform_device(self._h, Xc.data_ptr(), Xc.shape[0],
+                                                  Xc.shape[1] if Xc.dim() > 1 else 0,
+                                                  Y.data_ptr())
+                self._set_stream(None)
+            _lib.check(rc, self._h)
+            return Y
+        Xn = np.ascontiguousarray(X, dtype=np.float32)
+        if Xn.ndim != 2:
+            raise ValueError("X must be a 2-D array [n_samples, n_features]")
+        Y = np.empty((Xn.shape[0], self.d), dtype=np.float32)
+        rc = L.ncvis_fit_transform(self._h, Xn.ctypes.data, Xn.shape[0], Xn.shape[1],
+                                   Y.ctypes.data)
+        _lib.check(rc, self._h)
+        return Y
+
+    def stage_times(self) -> dict:
+        """Device times (ms) of the stages of the last fit_transform."""
+        t = _lib.NcvisStageTimes()
+        _lib.check(_lib.lib().ncvis_get_stage_times(self._h, C.byref(t)), self._h)
+        return t.as_dict()
+
+
+def _is_cuda_tensor(x) -> bool:
+    mod = type(x).__module__
+    return mod.startswith("torch") and getattr(x, "is_cuda", False)

@@ -1,0 +1,69 @@
+// Shared definitions for the NCVis GB300 engine: status codes, error
+// propagation, kernel-launch accounting, small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace ncvis_gpu {
+
+// Status codes returned through the C ABI (mirrored in include/ncvis_gb300.h).
+enum Status : int {
+    kOk = 0,
+    kInvalidArgument = 1,
+    kCudaError = 2,
+    kUnsupported = 3,
+    kDeviceTimeout = 4,
+    kInternal = 5,
+};
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &msg) : std::runtime_error(msg), code(c) {}
+};
+
+inline void check_cuda(cudaError_t e, const char *what, const char *file, int line) {
+    if (e != cudaSuccess) {
+        char buf[512];
+        snprintf(buf, sizeof(buf), "CUDA error %s (%d) in %s at %s:%d", cudaGetErrorString(e),
+                 (int)e, what, file, line);
+        throw Error(kCudaError, buf);
+    }
+}
+
+#define NCVIS_CUDA(call) ::ncvis_gpu::check_cuda((call), #call, __FILE__, __LINE__)
+
+inline void require(bool ok, const std::string &msg, int code = kInvalidArgument) {
+    if (!ok) throw Error(code, msg);
+}
+
+// Every kernel this library launches goes through NCVIS_LAUNCH, which counts
+// it; ncvis_kernel_launch_count() exposes the total so that a benchmark can
+// state how many engine kernels ran in a timed region.
+std::atomic<uint64_t> &launch_counter();
+
+#define NCVIS_LAUNCH(kernel, grid, block, smem, stream, ...)                        \
+    do {                                                                             \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                  \
+        ::ncvis_gpu::launch_counter().fetch_add(1, std::memory_order_relaxed);       \
+        NCVIS_CUDA(cudaGetLastError());                                              \
+    } while (0)
+
+inline int num_sms() {
+    static int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return sms;
+}
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace ncvis_gpu

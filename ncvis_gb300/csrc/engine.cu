@@ -1,0 +1,498 @@
+// The engine behind the C ABI (include/ncvis_gb300.h): parameter handling of
+// ncvis::NCVis (src/ncvis.cpp:12-21), the fit_transform pipeline
+// (src/ncvis.cpp:354-459) over the device stages, a growable device arena,
+// stage timing with CUDA events, and the handle-less stage entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ncvis_gb300.h"
+#include "common.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+std::atomic<uint64_t> &launch_counter() {
+    static std::atomic<uint64_t> counter{0};
+    return counter;
+}
+
+namespace {
+
+thread_local std::string g_last_error;
+
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Bump layout over one device allocation.
+struct Layout {
+    size_t total = 0;
+    size_t take(size_t bytes) {
+        size_t off = total;
+        total += align256(bytes);
+        return off;
+    }
+};
+
+struct Events {
+    cudaEvent_t ev[10];
+    Events() {
+        for (auto &e : ev) NCVIS_CUDA(cudaEventCreate(&e));
+    }
+    ~Events() {
+        for (auto &e : ev) cudaEventDestroy(e);
+    }
+    float ms(int a, int b) const {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[a], ev[b]);
+        return t;
+    }
+};
+
+}  // namespace
+
+}  // namespace ncvis_gpu
+
+using namespace ncvis_gpu;
+
+struct ncvis_engine {
+    ncvis_params p{};
+    std::vector<size_t> noise;
+    ncvis_options o{};
+    std::vector<int32_t> replay_stream;  // host copy of the recorded noise stream
+    std::string err;
+    ncvis_stage_times times{};
+    cudaStream_t own = nullptr;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+
+    // The engine's own stream is created on first use, so that constructing
+    // an engine touches no GPU (as constructing the reference's NCVis only
+    // stores parameters, src/ncvis.cpp:12-21).
+    cudaStream_t stream() {
+        if (o.stream) return (cudaStream_t)o.stream;
+        if (!own) NCVIS_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        return own;
+    }
+
+    ~ncvis_engine() {
+        if (arena) cudaFree(arena);
+        if (own) cudaStreamDestroy(own);
+    }
+
+    char *ensure_arena(size_t bytes) {
+        if (bytes > arena_bytes) {
+            if (arena) {
+                NCVIS_CUDA(cudaStreamSynchronize(stream()));
+                NCVIS_CUDA(cudaFree(arena));
+                arena = nullptr;
+                arena_bytes = 0;
+            }
+            NCVIS_CUDA(cudaMalloc(&arena, bytes));
+            arena_bytes = bytes;
+        }
+        return (char *)arena;
+    }
+
+    void fit(const float *X, size_t N, size_t D, float *Y, bool host);
+};
+
+namespace {
+
+// Checked when the engine is created: what the reference's constructor
+// itself cannot accept (it allocates n_epochs entries, src/ncvis.cpp:16).
+void check_params(const ncvis_params &p) {
+    require(p.n_epochs >= 0, "[ncvis] n_epochs must be non-negative");
+}
+
+template <class F>
+int guarded(ncvis_engine *h, F &&f) {
+    try {
+        f();
+        if (h) h->err.clear();
+        return NCVIS_OK;
+    } catch (const Error &e) {
+        if (h) h->err = e.what();
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::exception &e) {
+        if (h) h->err = e.what();
+        g_last_error = e.what();
+        return NCVIS_INTERNAL;
+    }
+}
+
+}  // namespace
+
+void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) {
+    if (N == 0 || D == 0)
+        throw Error(kInvalidArgument,
+                    "[ncvis::NCVis::fit_transform] Dataset should have at least one element.");
+    if (Y == nullptr)
+        throw Error(kInvalidArgument,
+                    "[ncvis::NCVis::fit_transform] Null pointer provided for output.");
+    require(X != nullptr, "[ncvis::NCVis::fit_transform] Null pointer provided for input.");
+    // The reference rejects an unknown distance when it builds the index
+    // (src/ncvis.cpp:89-90).
+    require(p.distance >= 0 && p.distance <= 3,
+            "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
+    require(p.d >= 1 && p.d <= 32, "[ncvis] embedding dimension d must be in [1, 32]");
+    require(p.n_init_epochs >= 0, "[ncvis] n_init_epochs must be non-negative");
+    require(N >= 2, "[ncvis::NCVis::fit_transform] Dataset should have at least two elements.");
+    require(N < (size_t(1) << 31) && D < (size_t(1) << 31), "[ncvis] N and D must be below 2^31");
+    // Number of neighbours cannot exceed the number of other points
+    // (src/ncvis.cpp:381-382).
+    size_t kk = (p.n_neighbors < N - 1) ? p.n_neighbors : (N - 1);
+    kk = (kk > 0) ? kk : 1;
+    require(kk <= 255, "[ncvis] n_neighbors above 255 is not supported");
+    const int k = (int)kk;
+    const int d = (int)p.d;
+    const int dist = p.distance;
+    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
+    require(!bf16, "[ncvis] the BF16 tensor-core kNN is not available in this build",
+            kUnsupported);
+    require((int64_t)N * k < (int64_t(1) << 30), "[ncvis] N * n_neighbors must be below 2^30");
+    require(host || ((uintptr_t)Y & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
+    const bool replay = (o.sgd_mode == NCVIS_SGD_REPLAY);
+
+    cudaStream_t s = stream();
+    KnnPlan kp = plan_knn_f32((int64_t)N, k, o.rerank_factor);
+    const int C = kp.C();
+    const int64_t nk = (int64_t)N * k;
+    const int chains = o.sgd_chains > 0 ? o.sgd_chains : sgd_default_chains(2 * nk);
+
+    Layout L;
+    const size_t o_X = host ? L.take(sizeof(float) * N * D) : 0;
+    const size_t o_Y = host ? L.take(sizeof(float) * N * d) : 0;
+    const size_t o_Xp = L.take(sizeof(float) * N * D);
+    const size_t o_sqn = L.take(sizeof(float) * N);
+    const size_t o_flag = L.take(sizeof(int) * 4);
+    const size_t o_ci = L.take(sizeof(int32_t) * N * C);
+    const size_t o_cd = L.take(sizeof(float) * N * C);
+    const size_t o_ki = L.take(sizeof(int32_t) * nk);
+    const size_t o_kd = L.take(sizeof(float) * nk);
+    const size_t o_rp = L.take(sizeof(int64_t) * (N + 1));
+    const size_t o_cols = L.take(sizeof(int32_t) * 2 * nk);
+    const size_t o_vals = L.take(sizeof(float) * 2 * nk);
+    const size_t o_src = L.take(sizeof(int32_t) * 2 * nk);
+    const size_t o_Q = L.take(sizeof(float) * 4);
+    const size_t o_sym = L.take(symmetrize_workspace_bytes((int64_t)N, k));
+    const size_t o_init = L.take(init_workspace_bytes((int64_t)N, d));
+    const size_t o_sgd = L.take(sgd_workspace_bytes(chains));
+    const size_t o_stream = replay ? L.take(sizeof(int32_t) * std::max<size_t>(o.replay_len, 1)) : 0;
+    char *base = ensure_arena(L.total);
+
+    const float *dX = host ? (float *)(base + o_X) : X;
+    float *dY = host ? (float *)(base + o_Y) : Y;
+    float *Xp = (float *)(base + o_Xp);
+    float *sqn = (float *)(base + o_sqn);
+    int *flag = (int *)(base + o_flag);
+    int32_t *cand_i = (int32_t *)(base + o_ci);
+    float *cand_d = (float *)(base + o_cd);
+    int32_t *knn_i = (int32_t *)(base + o_ki);
+    float *knn_d = (float *)(base + o_kd);
+    int64_t *row_ptr = (int64_t *)(base + o_rp);
+    int32_t *cols = (int32_t *)(base + o_cols);
+    float *vals = (float *)(base + o_vals);
+    int32_t *src = (int32_t *)(base + o_src);
+    float *dQ = (float *)(base + o_Q);
+
+    Events ev;
+    NCVIS_CUDA(cudaEventRecord(ev.ev[0], s));
+    if (host)
+        NCVIS_CUDA(cudaMemcpyAsync((void *)dX, X, sizeof(float) * N * D, cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
+    NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
+    launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, nullptr, 0, flag, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
+    {
+        int bad = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(bad == 0, "[ncvis] input contains non-finite values");
+    }
+    NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
+    launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
+    launch_rerank(Xp, (int64_t)N, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
+    const int64_t E = run_symmetrize((int64_t)N, k, knn_i, knn_d, base + o_sym, row_ptr, cols, vals,
+                                     src, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[5], s));
+
+    const float init_alpha = (float)(1. / k);
+    run_init_embedding((int64_t)N, d, row_ptr, cols, (uint64_t)p.random_seed, p.n_init_epochs,
+                       init_alpha, dY, base + o_init, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[6], s));
+
+    NCVIS_CUDA(cudaMemsetAsync(dQ, 0, sizeof(float), s));
+    SgdArgs g;
+    g.N = (int64_t)N;
+    g.d = d;
+    g.E = E;
+    g.src = src;
+    g.dst = cols;
+    g.Y = dY;
+    g.Q = dQ;
+    g.seed = (uint64_t)p.random_seed;
+    g.n_epochs = p.n_epochs;
+    g.a = p.a;
+    g.b = p.b;
+    g.alpha = p.alpha;
+    g.alpha_Q = p.alpha_Q;
+    if (replay) {
+        size_t need = 0;
+        for (int e = 0; e < p.n_epochs; ++e) need += (size_t)E * noise[e];
+        require(replay_stream.size() >= need,
+                "[ncvis] replay stream shorter than E * sum(n_noise) = " + std::to_string(need));
+        int32_t *dstream = (int32_t *)(base + o_stream);
+        if (need)
+            NCVIS_CUDA(cudaMemcpyAsync(dstream, replay_stream.data(), sizeof(int32_t) * need,
+                                       cudaMemcpyHostToDevice, s));
+        int *err = flag + 1;
+        size_t pos = 0;
+        for (int e = 0; e < p.n_epochs; ++e) {
+            launch_sgd_replay(g, e, noise[e], 0, E, dstream, (int64_t)pos, err, s);
+            pos += (size_t)E * noise[e];
+        }
+        int rerr = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&rerr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(rerr == 0, "[ncvis] replay stream holds an index outside [0, N)");
+    } else if (p.n_epochs > 0 && E > 0) {
+        run_sgd_hogwild(g, 0, p.n_epochs, noise.data(), chains, base + o_sgd, s);
+    }
+    NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
+    if (host)
+        NCVIS_CUDA(cudaMemcpyAsync(Y, dY, sizeof(float) * N * d, cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaEventRecord(ev.ev[8], s));
+    NCVIS_CUDA(cudaEventSynchronize(ev.ev[8]));
+
+    times.h2d_ms = ev.ms(0, 1);
+    times.preprocess_ms = ev.ms(1, 2);
+    times.knn_ms = ev.ms(2, 3);
+    times.rerank_ms = ev.ms(3, 4);
+    times.symmetrize_ms = ev.ms(4, 5);
+    times.build_edges_ms = 0.f;  // fused into the CSR compaction
+    times.init_ms = ev.ms(5, 6);
+    times.optimize_ms = ev.ms(6, 7);
+    times.d2h_ms = ev.ms(7, 8);
+    times.total_ms = ev.ms(0, 8);
+    times.n_edges = E;
+    times.k = k;
+}
+
+// ------------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+ncvis_handle ncvis_create(const ncvis_params *params, const ncvis_options *options) {
+    ncvis_engine *h = nullptr;
+    int rc = guarded(nullptr, [&] {
+        require(params != nullptr, "[ncvis] null parameters");
+        check_params(*params);
+        std::unique_ptr<ncvis_engine> e(new ncvis_engine());
+        e->p = *params;
+        // n_noise is copied; nullptr means 3 noise samples per epoch
+        // (src/ncvis.cpp:16-20).
+        e->noise.resize((size_t)params->n_epochs);
+        for (int i = 0; i < params->n_epochs; ++i)
+            e->noise[i] = params->n_noise ? params->n_noise[i] : 3;
+        e->p.n_noise = nullptr;
+        if (options) {
+            e->o = *options;
+            if (options->replay_stream && options->replay_len)
+                e->replay_stream.assign(options->replay_stream, options->replay_stream + options->replay_len);
+            e->o.replay_stream = nullptr;
+        }
+        h = e.release();
+    });
+    return rc == NCVIS_OK ? h : nullptr;
+}
+
+void ncvis_destroy(ncvis_handle h) { delete h; }
+
+int ncvis_set_options(ncvis_handle h, const ncvis_options *options) {
+    if (!h) return NCVIS_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        require(options != nullptr, "[ncvis] null options");
+        h->o = *options;
+        h->replay_stream.clear();
+        if (options->replay_stream && options->replay_len)
+            h->replay_stream.assign(options->replay_stream, options->replay_stream + options->replay_len);
+        h->o.replay_stream = nullptr;
+    });
+}
+
+int ncvis_fit_transform(ncvis_handle h, const float *X, size_t N, size_t D, float *Y) {
+    if (!h) return NCVIS_INVALID_ARGUMENT;
+    return guarded(h, [&] { h->fit(X, N, D, Y, true); });
+}
+
+int ncvis_fit_transform_device(ncvis_handle h, const float *dX, size_t N, size_t D, float *dY) {
+    if (!h) return NCVIS_INVALID_ARGUMENT;
+    return guarded(h, [&] { h->fit(dX, N, D, dY, false); });
+}
+
+const char *ncvis_last_error(ncvis_handle h) { return h ? h->err.c_str() : "null handle"; }
+
+const char *ncvis_get_last_error(void) { return g_last_error.c_str(); }
+
+int ncvis_get_stage_times(ncvis_handle h, ncvis_stage_times *out) {
+    if (!h || !out) return NCVIS_INVALID_ARGUMENT;
+    *out = h->times;
+    return NCVIS_OK;
+}
+
+int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
+                     int rerank_factor, int32_t *d_inds, float *d_dists, void *stream) {
+    return guarded(nullptr, [&] {
+        require(dX && d_inds && d_dists, "knn: null pointer");
+        require(N >= 2 && k >= 1 && k <= N - 1 && k <= 255, "knn: need 2 <= N and 1 <= k <= min(N-1, 255)");
+        require(D >= 1 && N < (size_t(1) << 31) && N * k < (size_t(1) << 30),
+                "knn: need D >= 1, N < 2^31 and N * k < 2^30");
+        require(distance >= 0 && distance <= 3, "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
+        require(precision == NCVIS_KNN_FP32, "knn: the BF16 tensor-core kNN is not available in this build",
+                kUnsupported);
+        cudaStream_t s = (cudaStream_t)stream;
+        KnnPlan kp = plan_knn_f32((int64_t)N, (int)k, rerank_factor);
+        const int C = kp.C();
+        Layout L;
+        const size_t o_Xp = L.take(sizeof(float) * N * D);
+        const size_t o_sqn = L.take(sizeof(float) * N);
+        const size_t o_flag = L.take(sizeof(int));
+        const size_t o_ci = L.take(sizeof(int32_t) * N * C);
+        const size_t o_cd = L.take(sizeof(float) * N * C);
+        char *base = nullptr;
+        NCVIS_CUDA(cudaMallocAsync((void **)&base, L.total, s));
+        NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int), s));
+        launch_preprocess(dX, (int64_t)N, (int)D, distance, (float *)(base + o_Xp),
+                          (float *)(base + o_sqn), nullptr, 0, (int *)(base + o_flag), s);
+        int bad = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&bad, base + o_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        if (bad) {
+            cudaFreeAsync(base, s);
+            throw Error(kInvalidArgument, "knn: input contains non-finite values");
+        }
+        NCVIS_CUDA(cudaMemsetAsync(d_inds, 0xff, sizeof(int32_t) * N * k, s));
+        launch_knn_select_f32((float *)(base + o_Xp), (float *)(base + o_sqn), (int64_t)N, (int)D,
+                              distance, kp, (int32_t *)(base + o_ci), (float *)(base + o_cd), s);
+        launch_rerank((float *)(base + o_Xp), (int64_t)N, (int)D, distance,
+                      (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s);
+        NCVIS_CUDA(cudaFreeAsync(base, s));
+    });
+}
+
+int ncvis_symmetrize_device(size_t N, size_t k, const int32_t *d_inds, const float *d_dists,
+                            int64_t *d_row_ptr, int32_t *d_cols, float *d_vals, int32_t *d_src,
+                            size_t *n_edges, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_inds && d_dists && d_row_ptr && d_cols && d_vals && n_edges,
+                "symmetrize: null pointer");
+        require(N >= 1 && k >= 1, "symmetrize: empty table");
+        cudaStream_t s = (cudaStream_t)stream;
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, symmetrize_workspace_bytes((int64_t)N, (int)k), s));
+        int64_t E = 0;
+        try {
+            E = run_symmetrize((int64_t)N, (int)k, d_inds, d_dists, ws, d_row_ptr, d_cols, d_vals,
+                               d_src, s);
+        } catch (...) {
+            cudaFreeAsync(ws, s);
+            throw;
+        }
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+        *n_edges = (size_t)E;
+    });
+}
+
+int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
+                                const int32_t *d_cols, uint64_t seed, int n_init_epochs,
+                                float alpha, float *dY, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_row_ptr && d_cols && dY, "init_embedding: null pointer");
+        require(N >= 1 && d >= 1 && d <= 32 && n_init_epochs >= 0,
+                "init_embedding: need N >= 1, 1 <= d <= 32, n_init_epochs >= 0");
+        cudaStream_t s = (cudaStream_t)stream;
+        // The graph must be a CSR over N rows: offsets from 0, non-decreasing,
+        // columns in [0, N).
+        std::vector<int64_t> rp(N + 1);
+        NCVIS_CUDA(cudaMemcpyAsync(rp.data(), d_row_ptr, sizeof(int64_t) * (N + 1),
+                                   cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(rp[0] == 0, "init_embedding: row_ptr[0] must be 0");
+        for (size_t i = 0; i < N; ++i)
+            require(rp[i + 1] >= rp[i], "init_embedding: row_ptr must be non-decreasing");
+        require(rp[N] < (int64_t(1) << 31), "init_embedding: too many edges");
+        require(indices_in_range(d_cols, rp[N], (int64_t)N, s),
+                "init_embedding: a column index is outside [0, N)");
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, init_workspace_bytes((int64_t)N, (int)d), s));
+        run_init_embedding((int64_t)N, (int)d, d_row_ptr, d_cols, seed, n_init_epochs, alpha, dY,
+                           ws, s);
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+    });
+}
+
+int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
+                          const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
+                          int epoch_begin, int epoch_end, int n_epochs, const size_t *n_noise,
+                          float a, float b, float alpha, float alpha_Q, int chains, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_dst && dY && dQ && n_noise, "optimize: null pointer");
+        require(N >= 2 && d >= 1 && d <= 32, "optimize: need N >= 2 and 1 <= d <= 32");
+        require(((uintptr_t)dY & 7) == 0, "optimize: Y must be 8-byte aligned");
+        require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
+                "optimize: need 0 <= epoch_begin <= epoch_end <= n_epochs");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (E == 0 || epoch_begin == epoch_end) return;
+        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
+                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+                "optimize: an edge endpoint is outside [0, N)");
+        if (chains <= 0) chains = sgd_default_chains((int64_t)E);
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
+        SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,
+                  a, b, alpha, alpha_Q};
+        run_sgd_hogwild(g, epoch_begin, epoch_end, n_noise, chains, ws, s);
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+    });
+}
+
+int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const int32_t *d_dst,
+                                 size_t edge_begin, size_t edge_end, const int32_t *d_stream,
+                                 size_t stream_offset, float *dY, float *dQ, int epoch,
+                                 int n_epochs, size_t n_noise_epoch, float a, float b, float alpha,
+                                 float alpha_Q, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_dst && dY && dQ, "optimize_replay: null pointer");
+        require(d_stream || n_noise_epoch == 0, "optimize_replay: null noise stream");
+        require(N >= 2 && d >= 1 && d <= 32, "optimize_replay: need N >= 2 and 1 <= d <= 32");
+        require(edge_begin <= edge_end && epoch >= 0 && epoch < n_epochs,
+                "optimize_replay: bad edge or epoch range");
+        cudaStream_t s = (cudaStream_t)stream;
+        int *err = nullptr;
+        NCVIS_CUDA(cudaMallocAsync((void **)&err, sizeof(int), s));
+        NCVIS_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+        SgdArgs g{(int64_t)N, (int)d, 0, d_src, d_dst, dY, dQ, 0, n_epochs, a, b, alpha, alpha_Q};
+        launch_sgd_replay(g, epoch, n_noise_epoch, (int64_t)edge_begin, (int64_t)edge_end,
+                          d_stream, (int64_t)stream_offset, err, s);
+        int herr = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaFreeAsync(err, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(herr == 0, "optimize_replay: an index outside [0, N) was met; replay stopped");
+    });
+}
+
+uint64_t ncvis_kernel_launch_count(void) { return launch_counter().load(); }
+
+const char *ncvis_version(void) { return "ncvis_gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,303 @@
+// K3 + K4: exact kNN in FP32, the plain drop-in replacement for the
+// reference's HNSW build and query (src/ncvis.cpp:72-153).
+//
+// K3 (knn_select_f32): a tiled FP32 FFMA distance GEMM.  A block owns 64
+// query points and sweeps one candidate range in tiles of 128; each thread
+// accumulates a 4 x 8 patch of dot products.  Distances use the GEMM forms
+// |q|^2 + |c|^2 - 2<q,c> (squared L2) and 1 - <q,c> (inner-product spaces).
+// Every query keeps a sorted list of its R best (distance, index) pairs in
+// shared memory; a tile's distances pass a per-query threshold filter into a
+// per-query buffer and are merged into the list between tiles.  Large
+// problems use one candidate range; small ones split the range so that the
+// grid fills the GPU, and K4 merges the splits.
+//
+// K4 (rerank): one warp per point recomputes the exact distance of each
+// candidate the way the hnswlib spaces do (sum of squared differences, or
+// 1 - dot, accumulated left to right in FP32), ranks the candidates by
+// (distance, index), drops rank 0 and writes ranks k..1, i.e. the k farthest
+// of the k+1 nearest in descending order, as findKNN stores them.
+#include <algorithm>
+#include <cfloat>
+
+#include "common.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+namespace {
+
+constexpr int BM = 64;   // queries per block
+constexpr int BN = 128;  // candidates per tile
+constexpr int BK = 16;   // reduction slice
+constexpr int NT = 256;  // threads per block
+
+__device__ __forceinline__ bool pair_less(float da, int ia, float db, int ib) {
+    return da < db || (da == db && ia < ib);
+}
+
+struct SelectSmem {
+    float *As;     // [BK][BM]
+    float *Bs;     // [BK][BN]
+    float *lst_d;  // [R][BM]
+    int *lst_i;    // [R][BM]
+    float *buf_d;  // [BN][BM]
+    int *buf_i;    // [BN][BM]
+    int *lst_n;    // [BM]
+    int *buf_n;    // [BM]
+    float *thr;    // [BM]
+};
+
+__host__ __device__ inline size_t select_smem_bytes(int R) {
+    return sizeof(float) * (BK * BM + BK * BN) + (sizeof(float) + sizeof(int)) * (size_t)R * BM +
+           (sizeof(float) + sizeof(int)) * (size_t)BN * BM + sizeof(int) * 2 * BM +
+           sizeof(float) * BM;
+}
+
+__device__ inline SelectSmem carve(char *base, int R) {
+    SelectSmem s;
+    s.As = (float *)base;
+    s.Bs = s.As + BK * BM;
+    s.lst_d = s.Bs + BK * BN;
+    s.lst_i = (int *)(s.lst_d + R * BM);
+    s.buf_d = (float *)(s.lst_i + R * BM);
+    s.buf_i = (int *)(s.buf_d + BN * BM);
+    s.lst_n = s.buf_i + BN * BM;
+    s.buf_n = s.lst_n + BM;
+    s.thr = (float *)(s.buf_n + BM);
+    return s;
+}
+
+__global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ Xp,
+                                                     const float *__restrict__ sqnorm, int64_t N,
+                                                     int D, int dist, int R, int splits,
+                                                     int32_t *__restrict__ cand_i,
+                                                     float *__restrict__ cand_d) {
+    extern __shared__ __align__(16) char smem_raw[];
+    SelectSmem sm = carve(smem_raw, R);
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int64_t q0 = (int64_t)blockIdx.x * BM;
+    const int split = blockIdx.y;
+    const int64_t c_begin = N * split / splits;
+    const int64_t c_end = N * (split + 1) / splits;
+    const bool l2 = (dist == kSquaredL2);
+
+    if (tid < BM) {
+        sm.lst_n[tid] = 0;
+        sm.buf_n[tid] = 0;
+        sm.thr[tid] = FLT_MAX;
+    }
+    float qn[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        int64_t q = q0 + ty * 4 + i;
+        qn[i] = (q < N) ? sqnorm[q] : 0.f;
+    }
+    __syncthreads();
+
+    for (int64_t c0 = c_begin; c0 < c_end; c0 += BN) {
+        float acc[4][8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+        for (int k0 = 0; k0 < D; k0 += BK) {
+            {  // queries: 64 rows x 16 columns, 4 per thread
+                const int q = tid >> 2, kk = (tid & 3) * 4;
+                const int64_t gq = q0 + q;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int kc = k0 + kk + j;
+                    sm.As[(kk + j) * BM + q] = (gq < N && kc < D) ? Xp[gq * D + kc] : 0.f;
+                }
+            }
+            {  // candidates: 128 rows x 16 columns, 8 per thread
+                const int c = tid >> 1, kk = (tid & 1) * 8;
+                const int64_t gc = c0 + c;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int kc = k0 + kk + j;
+                    sm.Bs[(kk + j) * BN + c] = (gc < c_end && kc < D) ? Xp[gc * D + kc] : 0.f;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int kk = 0; kk < BK; ++kk) {
+                const float4 a = *reinterpret_cast<const float4 *>(&sm.As[kk * BM + ty * 4]);
+                float b[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) b[j] = sm.Bs[kk * BN + tx + 16 * j];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    acc[0][j] = fmaf(a.x, b[j], acc[0][j]);
+                    acc[1][j] = fmaf(a.y, b[j], acc[1][j]);
+                    acc[2][j] = fmaf(a.z, b[j], acc[2][j]);
+                    acc[3][j] = fmaf(a.w, b[j], acc[3][j]);
+                }
+            }
+            __syncthreads();
+        }
+
+        // Threshold filter into the per-query buffers.
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t gc = c0 + tx + 16 * j;
+            if (gc >= c_end) continue;
+            const float cn = l2 ? sqnorm[gc] : 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int q = ty * 4 + i;
+                if (q0 + q >= N) continue;
+                const float dv = l2 ? (qn[i] + cn) - 2.f * acc[i][j] : 1.f - acc[i][j];
+                if (dv <= sm.thr[q]) {
+                    const int slot = atomicAdd(&sm.buf_n[q], 1);
+                    sm.buf_d[slot * BM + q] = dv;
+                    sm.buf_i[slot * BM + q] = (int)gc;
+                }
+            }
+        }
+        __syncthreads();
+
+        // Merge each query's buffer into its sorted list.
+        if (tid < BM) {
+            const int q = tid;
+            int n = sm.lst_n[q];
+            const int nb = sm.buf_n[q];
+            for (int t = 0; t < nb; ++t) {
+                const float dv = sm.buf_d[t * BM + q];
+                const int iv = sm.buf_i[t * BM + q];
+                if (n == R) {
+                    if (!pair_less(dv, iv, sm.lst_d[(R - 1) * BM + q], sm.lst_i[(R - 1) * BM + q]))
+                        continue;
+                    --n;
+                }
+                int p = n;
+                while (p > 0 && pair_less(dv, iv, sm.lst_d[(p - 1) * BM + q],
+                                          sm.lst_i[(p - 1) * BM + q])) {
+                    sm.lst_d[p * BM + q] = sm.lst_d[(p - 1) * BM + q];
+                    sm.lst_i[p * BM + q] = sm.lst_i[(p - 1) * BM + q];
+                    --p;
+                }
+                sm.lst_d[p * BM + q] = dv;
+                sm.lst_i[p * BM + q] = iv;
+                ++n;
+            }
+            sm.lst_n[q] = n;
+            sm.buf_n[q] = 0;
+            sm.thr[q] = (n == R) ? sm.lst_d[(R - 1) * BM + q] : FLT_MAX;
+        }
+        __syncthreads();
+    }
+
+    // Write this split's list; empty slots are marked with index -1.
+    const int C = R * splits;
+    for (int t = tid; t < BM * R; t += NT) {
+        const int q = t % BM, p = t / BM;
+        const int64_t gq = q0 + q;
+        if (gq >= N) continue;
+        const bool have = p < sm.lst_n[q];
+        cand_i[gq * C + (int64_t)split * R + p] = have ? sm.lst_i[p * BM + q] : -1;
+        cand_d[gq * C + (int64_t)split * R + p] = have ? sm.lst_d[p * BM + q] : FLT_MAX;
+    }
+}
+
+// One warp per point.  Candidate distances are recomputed exactly, then
+// ranked; C <= 1024.
+__global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp, int64_t N, int D,
+                                                   int dist, const int32_t *__restrict__ cand_i,
+                                                   int C, int k, int32_t *__restrict__ inds,
+                                                   float *__restrict__ dists) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    float *sd = (float *)smem_raw + (size_t)warp * C * 2;
+    int *si = (int *)(sd + C);
+    if (row >= N) return;
+    const float *q = Xp + row * D;
+    for (int c = lane; c < C; c += 32) {
+        const int idx = cand_i[row * C + c];
+        float dv = FLT_MAX;
+        if (idx >= 0) {
+            const float *y = Xp + (int64_t)idx * D;
+            float acc = 0.f;
+            if (dist == kSquaredL2) {
+                for (int t = 0; t < D; ++t) {
+                    const float diff = __fsub_rn(q[t], y[t]);
+                    acc = __fadd_rn(acc, __fmul_rn(diff, diff));
+                }
+                dv = acc;
+            } else {
+                for (int t = 0; t < D; ++t) acc = __fadd_rn(acc, __fmul_rn(q[t], y[t]));
+                dv = __fsub_rn(1.f, acc);
+            }
+        }
+        sd[c] = dv;
+        si[c] = idx;
+    }
+    __syncwarp();
+    for (int c = lane; c < C; c += 32) {
+        const int idx = si[c];
+        if (idx < 0) continue;
+        const float dv = sd[c];
+        int rank = 0;
+        for (int t = 0; t < C; ++t) {
+            const int it = si[t];
+            rank += (it >= 0 && pair_less(sd[t], it, dv, idx)) ? 1 : 0;
+        }
+        if (rank >= 1 && rank <= k) {
+            inds[row * k + (k - rank)] = idx;
+            dists[row * k + (k - rank)] = dv;
+        }
+    }
+}
+
+}  // namespace
+
+KnnPlan plan_knn_f32(int64_t N, int k, int rerank_factor) {
+    KnnPlan p;
+    if (rerank_factor <= 0) rerank_factor = 2;
+    int64_t R = std::max<int64_t>((int64_t)rerank_factor * k, (int64_t)k + 1);
+    R = std::min<int64_t>(R, N);
+    R = std::min<int64_t>(R, 256);
+    p.R = (int)R;
+    // Split the candidate range until the grid covers the GPU twice.
+    const int64_t tiles = (N + BM - 1) / BM;
+    int splits = 1;
+    while (tiles * splits < 2 * num_sms() && splits * 2 * p.R <= 1024 &&
+           N / (splits * 2) >= BN)
+        splits *= 2;
+    p.splits = splits;
+    return p;
+}
+
+void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int D, int dist,
+                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s) {
+    const size_t smem = select_smem_bytes(plan.R);
+    static size_t configured = 0;
+    if (smem > configured) {
+        NCVIS_CUDA(cudaFuncSetAttribute(knn_select_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        configured = smem;
+    }
+    dim3 grid(ceil_div(N, BM), plan.splits);
+    NCVIS_LAUNCH(knn_select_f32, grid, NT, smem, s, Xp, sqnorm, N, D, dist, plan.R, plan.splits,
+                 cand_i, cand_d);
+}
+
+void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,
+                   int k, int32_t *inds, float *dists, cudaStream_t s) {
+    require(C <= 1024, "rerank: too many candidates per point");
+    const int warps = 4;
+    const size_t smem = (size_t)warps * C * 8;
+    static size_t configured = 0;
+    if (smem > configured) {
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        configured = smem;
+    }
+    NCVIS_LAUNCH(rerank_rows, ceil_div(N, warps), warps * 32, smem, s, Xp, N, D, dist, cand_i, C,
+                 k, inds, dists);
+}
+
+}  // namespace ncvis_gpu

@@ -1,0 +1,422 @@
+// K7: NCVis::optimize (src/ncvis.cpp:275-352), noise-contrastive SGD on the
+// embedding Y and the learnable log-normaliser Q.
+//
+// Per epoch e: step = alpha (1 - (e/n_epochs)^2); every positive edge (i, j)
+// is followed by nu_e noise samples o ~ U{0..N-1} \ {i}; for each sample
+//   d2 = |y_i - y_o|^2,  Ph = 1 / (1 + a d2^b),
+//   w  = 1/(1 + Ph/(nu e^Q)) (positive) | -1/(1 + nu e^Q / Ph) (noise),
+//   Q -= alpha_Q w,   w <- 2 w Ph a b d2^(b-1)   (w = 1 when nu == 0),
+//   dx = clip((y_o - y_i) w step, +-4),  y_i += dx,  y_o -= dx.
+//
+// Hogwild mode (sgd_epoch): the reference runs this lock-free on OpenMP
+// threads, each with a private copy of Q over a contiguous chunk of the edge
+// list, and averages the copies at the end of the epoch.  Here each GPU
+// thread is such a chain: a contiguous chunk of edges, a private Q copy, and
+// Philox4x32-10 noise keyed by (seed) and counted by (edge, epoch, sample
+// pair, retry); the chains' copies are averaged in FP64 by reduce_q.  Y is
+// read and written through L2 (ld/st.cg) so that chains on other SMs see each
+// other's updates as the reference's threads do.
+//
+// Replay mode (sgd_replay): one thread executes the one-thread reference
+// sample by sample, with the reference build's arithmetic grouping (noise
+// weight -1/(nu e^Q (1 + a d2^b) + 1), final weight (w d2^(b-1)) ((a b)(Ph+Ph)),
+// w*step formed once) in round-to-nearest without contraction, powers and
+// exponentials evaluated in double and rounded once, and the noise indices
+// read from a recorded stream.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "common.cuh"
+#include "rng.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int D>
+struct Vec {
+    float v[D];
+};
+
+template <int D>
+__device__ __forceinline__ Vec<D> load_row(const float *Y, int64_t i) {
+    Vec<D> r;
+    if constexpr (D == 2) {
+        float2 t = __ldcg(reinterpret_cast<const float2 *>(Y + i * 2));
+        r.v[0] = t.x;
+        r.v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) r.v[c] = __ldcg(Y + i * D + c);
+    }
+    return r;
+}
+
+template <int D>
+__device__ __forceinline__ void store_row(float *Y, int64_t i, const Vec<D> &r) {
+    if constexpr (D == 2) {
+        __stcg(reinterpret_cast<float2 *>(Y + i * 2), make_float2(r.v[0], r.v[1]));
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) __stcg(Y + i * D + c, r.v[c]);
+    }
+}
+
+struct EpochConst {
+    float step, nu_f, a, b, ab, alpha_Q, pow_b1_at_zero;
+    int nu;
+};
+
+// The update weight of one sample (w * step), Q copy updated in place.
+__device__ __forceinline__ float nce_weight(float d2, bool positive, const EpochConst &k,
+                                            float &Qc) {
+    if (k.nu == 0) return k.step;
+    float p, p1;
+    if (d2 > 0.f) {
+        p = exp2f(k.b * __log2f(d2));
+        p1 = __fdividef(p, d2);
+    } else {
+        p = 0.f;
+        p1 = k.pow_b1_at_zero;
+    }
+    const float denom = fmaf(k.a, p, 1.f);
+    const float ph = __frcp_rn(denom);
+    const float nm = k.nu_f * __expf(Qc);
+    float w = positive ? __frcp_rn(__fdividef(ph, nm) + 1.f) : -__frcp_rn(fmaf(nm, denom, 1.f));
+    Qc = fmaf(-w, k.alpha_Q, Qc);
+    w = w * p1 * (2.f * k.ab * ph);
+    return w * k.step;
+}
+
+template <int D>
+__device__ __forceinline__ float sq_dist(const Vec<D> &x, const Vec<D> &y) {
+    float d2 = 0.f;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        const float t = x.v[c] - y.v[c];
+        d2 = fmaf(t, t, d2);
+    }
+    return d2;
+}
+
+__device__ __forceinline__ float clip4(float v) { return fminf(fmaxf(v, -4.f), 4.f); }
+
+// y_i += dx, y_o -= dx on distinct rows.
+template <int D>
+__device__ __forceinline__ void apply(Vec<D> &yi, Vec<D> &yo, float ws) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        const float dx = clip4((yo.v[c] - yi.v[c]) * ws);
+        yi.v[c] += dx;
+        yo.v[c] -= dx;
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
+                                                      const int32_t *__restrict__ src,
+                                                      const int32_t *__restrict__ dst, int64_t E,
+                                                      uint32_t N, const float *__restrict__ Q_in,
+                                                      double *__restrict__ q_part, EpochConst k,
+                                                      int epoch, uint32_t key0, uint32_t key1,
+                                                      int64_t chunk) {
+    const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const int64_t e0 = chain * chunk;
+    const int64_t e1 = min(E, e0 + chunk);
+    float Qc = *Q_in;
+    for (int64_t e = e0; e < e1; ++e) {
+        const int32_t i = src[e];
+        const int32_t j = dst[e];
+        Vec<D> yi = load_row<D>(Y, i);
+        if (j != i) {
+            Vec<D> yo = load_row<D>(Y, j);
+            apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), true, k, Qc));
+            store_row<D>(Y, j, yo);
+        } else {
+            // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
+            const float ws = nce_weight(0.f, true, k, Qc);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const float dx = clip4(0.f * ws);
+                yi.v[c] = (yi.v[c] + dx) - dx;
+            }
+        }
+        for (int s = 0; s < k.nu; s += 2) {
+            uint32_t retry = 0;
+            Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)epoch,
+                                         (uint32_t)(s >> 1), key0, key1);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (s + h >= k.nu) break;
+                uint32_t o = bounded_index(r.v[2 * h], r.v[2 * h + 1], N);
+                while (o == (uint32_t)i) {  // redraw, as the reference does
+                    if (++retry > 64) {  // P = N^-64: never in practice; keeps the loop finite
+                        o = (o + 1 == N) ? 0 : o + 1;
+                        break;
+                    }
+                    Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16),
+                                                  (uint32_t)epoch, (uint32_t)(s >> 1) | 0x80000000u,
+                                                  key0 ^ retry, key1);
+                    o = bounded_index(rr.v[0], rr.v[1], N);
+                }
+                Vec<D> yo = load_row<D>(Y, o);
+                apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), false, k, Qc));
+                store_row<D>(Y, o, yo);
+            }
+        }
+        store_row<D>(Y, i, yi);
+    }
+    // Chain copies of Q, summed in FP64 per block.
+    __shared__ double red[kThreads / 32];
+    double v = Qc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+        q_part[blockIdx.x] = t;
+    }
+}
+
+// Runtime-d variant (d > 4).
+__global__ void __launch_bounds__(kThreads) sgd_epoch_generic(
+    float *__restrict__ Y, int d, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
+    int64_t E, uint32_t N, const float *__restrict__ Q_in, double *__restrict__ q_part, EpochConst k,
+    int epoch, uint32_t key0, uint32_t key1, int64_t chunk) {
+    const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const int64_t e0 = chain * chunk;
+    const int64_t e1 = min(E, e0 + chunk);
+    float Qc = *Q_in;
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t i = src[e];
+        for (int s = 0; s <= k.nu; ++s) {
+            int64_t o;
+            if (s == 0) {
+                o = dst[e];
+            } else {
+                const int sn = s - 1;
+                Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)epoch,
+                                             (uint32_t)(sn >> 1), key0, key1);
+                o = bounded_index(r.v[2 * (sn & 1)], r.v[2 * (sn & 1) + 1], N);
+                uint32_t retry = 0;
+                while (o == i) {
+                    if (++retry > 64) {
+                        o = (o + 1 == (int64_t)N) ? 0 : o + 1;
+                        break;
+                    }
+                    Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16),
+                                                  (uint32_t)epoch, (uint32_t)(sn >> 1) | 0x80000000u,
+                                                  key0 ^ retry, key1);
+                    o = bounded_index(rr.v[0], rr.v[1], N);
+                }
+            }
+            float d2 = 0.f;
+            for (int c = 0; c < d; ++c) {
+                const float t = __ldcg(Y + i * d + c) - __ldcg(Y + o * d + c);
+                d2 = fmaf(t, t, d2);
+            }
+            const float ws = nce_weight(d2, s == 0, k, Qc);
+            for (int c = 0; c < d; ++c) {
+                const float dx = clip4((__ldcg(Y + o * d + c) - __ldcg(Y + i * d + c)) * ws);
+                __stcg(Y + i * d + c, __ldcg(Y + i * d + c) + dx);
+                __stcg(Y + o * d + c, __ldcg(Y + o * d + c) - dx);
+            }
+        }
+    }
+    __shared__ double red[kThreads / 32];
+    double v = Qc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+        q_part[blockIdx.x] = t;
+    }
+}
+
+// Q = (sum of the chains' copies) / chains, as the reference's epoch-end
+// average over threads (src/ncvis.cpp:342-349).
+__global__ void reduce_q(const double *__restrict__ q_part, int blocks, int64_t chains,
+                         float *__restrict__ Q) {
+    __shared__ double red[32];
+    double s = 0;
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) s += q_part[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        *Q = (float)(t / (double)chains);
+    }
+}
+
+// ---------------------------------------------------------------- replay
+
+// The reference build's d_sqr: left to right for d <= 3; for d >= 4 four
+// running lane sums over the first 4*floor(d/4) coordinates, folded as
+// (l0 + l2) + (l1 + l3), the remainder added pairwise into the folded lanes.
+__device__ float replay_sq_dist(const float *x, const float *y, int d) {
+    float lane[4] = {0.f, 0.f, 0.f, 0.f};
+    const int body = (d >= 4) ? (d / 4) * 4 : 0;
+    for (int t = 0; t < body; t += 4)
+        for (int l = 0; l < 4; ++l) {
+            const float u = __fsub_rn(x[t + l], y[t + l]);
+            lane[l] = __fadd_rn(lane[l], __fmul_rn(u, u));
+        }
+    float f0 = __fadd_rn(lane[0], lane[2]);
+    float f1 = __fadd_rn(lane[1], lane[3]);
+    int t = body;
+    const int rem = d - body;
+    if (rem >= 2) {
+        const float u0 = __fsub_rn(x[t], y[t]), u1 = __fsub_rn(x[t + 1], y[t + 1]);
+        f0 = __fadd_rn(__fmul_rn(u0, u0), f0);
+        f1 = __fadd_rn(__fmul_rn(u1, u1), f1);
+        t += 2;
+    }
+    float acc = __fadd_rn(f0, f1);
+    if (t < d) {
+        const float u = __fsub_rn(x[t], y[t]);
+        acc = __fadd_rn(acc, __fmul_rn(u, u));
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void replay_sample(float *Y, int d, int64_t i, int64_t o, bool positive,
+                                              uint64_t nu, float a, float b, float alpha_Q,
+                                              float step, float &Qc) {
+    const float d2 = replay_sq_dist(Y + i * d, Y + o * d, d);
+    float w = 1.f;
+    if (nu != 0) {
+        const float p = (float)pow((double)d2, (double)b);
+        const float denom = __fadd_rn(__fmul_rn(a, p), 1.f);
+        const float ph = __fdiv_rn(1.f, denom);
+        const float ab2ph = __fmul_rn(__fmul_rn(a, b), __fadd_rn(ph, ph));
+        const float nm = __fmul_rn((float)nu, (float)exp((double)Qc));
+        w = positive ? __fdiv_rn(1.f, __fadd_rn(__fdiv_rn(ph, nm), 1.f))
+                     : __fdiv_rn(-1.f, __fadd_rn(__fmul_rn(nm, denom), 1.f));
+        Qc = __fsub_rn(Qc, __fmul_rn(w, alpha_Q));
+        const float p1 = (float)pow((double)d2, (double)__fsub_rn(b, 1.f));
+        w = __fmul_rn(__fmul_rn(w, p1), ab2ph);
+    }
+    const float ws = __fmul_rn(w, step);
+    for (int c = 0; c < d; ++c) {
+        float dx = __fmul_rn(__fsub_rn(Y[o * d + c], Y[i * d + c]), ws);
+        dx = fminf(fmaxf(dx, -4.f), 4.f);
+        Y[i * d + c] = __fadd_rn(Y[i * d + c], dx);
+        Y[o * d + c] = __fsub_rn(Y[o * d + c], dx);
+    }
+}
+
+// Indices outside [0, N) stop the replay and set *err (no write happens).
+__global__ void sgd_replay(float *Y, int64_t N, int d, const int32_t *__restrict__ src,
+                           const int32_t *__restrict__ dst, int64_t e0, int64_t e1,
+                           const int32_t *__restrict__ stream, int64_t pos, float *Q, int epoch,
+                           int n_epochs, uint64_t nu, float a, float b, float alpha, float alpha_Q,
+                           int *err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float frac = __fdiv_rn((float)epoch, (float)n_epochs);
+    const float step = __fmul_rn(alpha, __fsub_rn(1.f, __fmul_rn(frac, frac)));
+    float Qc = *Q;
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t i = src[e], j = dst[e];
+        if (i < 0 || i >= N || j < 0 || j >= N) {
+            *err = 1;
+            return;
+        }
+        replay_sample(Y, d, i, j, true, nu, a, b, alpha_Q, step, Qc);
+        for (uint64_t s = 0; s < nu; ++s) {
+            const int64_t o = stream[pos++];
+            if (o < 0 || o >= N) {
+                *err = 1;
+                return;
+            }
+            replay_sample(Y, d, i, o, false, nu, a, b, alpha_Q, step, Qc);
+        }
+    }
+    *Q = Qc;
+}
+
+EpochConst epoch_const(const SgdArgs &g, int epoch, int nu) {
+    EpochConst k;
+    const float frac = (float)epoch / (float)g.n_epochs;
+    k.step = g.alpha * (1.f - frac * frac);
+    k.nu = nu;
+    k.nu_f = (float)nu;
+    k.a = g.a;
+    k.b = g.b;
+    k.ab = g.a * g.b;
+    k.alpha_Q = g.alpha_Q;
+    k.pow_b1_at_zero = std::pow(0.f, g.b - 1.f);
+    return k;
+}
+
+}  // namespace
+
+int sgd_default_chains(int64_t E) {
+    // Enough chains to fill the GPU, but at least ~64 edges each so that a
+    // chain's Q copy follows many samples before the epoch average.
+    int64_t chains = (int64_t)num_sms() * 1024;
+    chains = std::min<int64_t>(chains, std::max<int64_t>(E / 64, 1));
+    return (int)std::max<int64_t>(chains, 1);
+}
+
+size_t sgd_workspace_bytes(int chains) {
+    return sizeof(double) * ((chains + kThreads - 1) / kThreads + 1);
+}
+
+void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const size_t *n_noise,
+                     int chains, void *workspace, cudaStream_t s) {
+    require(g.N >= 2 && g.N < (int64_t(1) << 31), "optimize: N must be in [2, 2^31)");
+    if (chains <= 0) chains = sgd_default_chains(g.E);
+    const int blocks = (int)ceil_div(chains, kThreads);
+    const int64_t total_chains = (int64_t)blocks * kThreads;
+    const int64_t chunk = (g.E + total_chains - 1) / total_chains;
+    double *q_part = (double *)workspace;
+    const uint32_t key0 = (uint32_t)g.seed, key1 = (uint32_t)(g.seed >> 32) ^ 0x5eed1u;
+    for (int ep = epoch_begin; ep < epoch_end; ++ep) {
+        const int nu = (int)n_noise[ep];
+        EpochConst k = epoch_const(g, ep, nu);
+        switch (g.d) {
+            case 1:
+                NCVIS_LAUNCH(sgd_epoch<1>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                break;
+            case 2:
+                NCVIS_LAUNCH(sgd_epoch<2>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                break;
+            case 3:
+                NCVIS_LAUNCH(sgd_epoch<3>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                break;
+            case 4:
+                NCVIS_LAUNCH(sgd_epoch<4>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                break;
+            default:
+                NCVIS_LAUNCH(sgd_epoch_generic, blocks, kThreads, 0, s, g.Y, g.d, g.src, g.dst,
+                             g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+        }
+        NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, blocks, total_chains, g.Q);
+    }
+}
+
+void launch_sgd_replay(const SgdArgs &g, int epoch, size_t nu, int64_t edge_begin,
+                       int64_t edge_end, const int32_t *stream, int64_t stream_offset, int *err,
+                       cudaStream_t s) {
+    NCVIS_LAUNCH(sgd_replay, 1, 32, 0, s, g.Y, g.N, g.d, g.src, g.dst, edge_begin, edge_end,
+                 stream, stream_offset, g.Q, epoch, g.n_epochs, (uint64_t)nu, g.a, g.b, g.alpha,
+                 g.alpha_Q, err);
+}
+
+}  // namespace ncvis_gpu

@@ -1,0 +1,93 @@
+// Host-side launchers of the engine's stages.  Every launcher only enqueues
+// work on `stream` (no synchronisation) unless its comment says otherwise.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace ncvis_gpu {
+
+enum Distance { kSquaredL2 = 0, kInnerProduct = 1, kCosine = 2, kCorrelation = 3 };
+
+// ---- K1 preprocess (src/ncvis.cpp:32-70) -------------------------------------
+// Xp[N, D] f32 preprocessed rows, sqnorm[N] = |xp|^2, and (if Xb != nullptr)
+// Xb[N, ldb] bf16 copies zero-padded to ldb columns.  bad_flag (device int)
+// is set to 1 if any input is not finite.
+void launch_preprocess(const float *X, int64_t N, int D, int dist, float *Xp, float *sqnorm,
+                       __nv_bfloat16 *Xb, int ldb, int *bad_flag, cudaStream_t s);
+
+// ---- K3 exact FP32 candidate selection + K4 rerank ---------------------------
+struct KnnPlan {
+    int R;       // candidates kept per (point, split)
+    int splits;  // candidate-range splits
+    int C() const { return R * splits; }
+};
+KnnPlan plan_knn_f32(int64_t N, int k, int rerank_factor);
+// cand_i/cand_d: [N, plan.C()]; -1 marks an empty slot.
+void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int D, int dist,
+                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s);
+// Exact distances of the candidates, top k+1 by (distance, index), smallest
+// dropped, k written in descending order: inds/dists [N, k].
+void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,
+                   int k, int32_t *inds, float *dists, cudaStream_t s);
+
+// ---- K2 BF16 tensor-core candidate selection ---------------------------------
+struct KnnTcPlan {
+    int R;       // candidates kept per point (multiple of 4 is not required)
+    int ldb;     // padded row length of Xb (bf16 elements)
+    int64_t Npad;
+};
+KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor);
+bool knn_tc_supported(int D, int R);
+void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
+                          const KnnTcPlan &plan, int dist, int32_t *cand_i, float *cand_d,
+                          int *timeout_flag, cudaStream_t s);
+
+// ---- K5 symmetrize (src/knntable.cpp:24-99, src/ncvis.cpp:155-173) -----------
+size_t symmetrize_workspace_bytes(int64_t N, int k);
+// Enqueues the CSR build and returns E (waits on the stream for the count).
+int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists, void *workspace,
+                       int64_t *row_ptr, int32_t *cols, float *vals, int32_t *src,
+                       cudaStream_t s);
+
+// True when every a[0..n) lies in [0, N) (waits on the stream).
+bool indices_in_range(const int32_t *a, int64_t n, int64_t N, cudaStream_t s);
+
+// ---- device-wide exclusive scan ----------------------------------------------
+size_t scan_workspace_bytes(int64_t n);
+// out[0..n]: out[0] = 0, out[i+1] = out[i] + in[i].
+void launch_exclusive_scan_i32_to_i64(const int32_t *in, int64_t *out, int64_t n, void *ws,
+                                      cudaStream_t s);
+
+// ---- K6 init (src/ncvis.cpp:184-273) ------------------------------------------
+size_t init_workspace_bytes(int64_t N, int d);
+void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t *cols,
+                        uint64_t seed, int n_init_epochs, float alpha, float *Y, void *workspace,
+                        cudaStream_t s);
+
+// ---- K7 SGD (src/ncvis.cpp:275-352) -------------------------------------------
+struct SgdArgs {
+    int64_t N;
+    int d;
+    int64_t E;
+    const int32_t *src;
+    const int32_t *dst;
+    float *Y;
+    float *Q;  // device scalar
+    uint64_t seed;
+    int n_epochs;
+    float a, b, alpha, alpha_Q;
+};
+size_t sgd_workspace_bytes(int chains);
+int sgd_default_chains(int64_t E);
+void run_sgd_hogwild(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
+                     int chains, void *workspace, cudaStream_t s);
+// *err (device int) is set to 1 if an index outside [0, N) is met.
+void launch_sgd_replay(const SgdArgs &args, int epoch, size_t nu, int64_t edge_begin,
+                       int64_t edge_end, const int32_t *stream, int64_t stream_offset, int *err,
+                       cudaStream_t s);
+
+}  // namespace ncvis_gpu

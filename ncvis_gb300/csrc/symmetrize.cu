@@ -1,0 +1,273 @@
+// K5: symmetrization of the kNN table into CSR, bit-exact with the
+// reference's KNNTable::symmetrize run on one thread (src/knntable.cpp:24-99)
+// followed by NCVis::build_edges (src/ncvis.cpp:155-173).
+//
+// The reference's row i after symmetrization is computed from
+//   row  = its k table entries, then every incoming entry (s, j) with
+//          inds[s][j] == i in increasing (s, j) order (one thread pushes them
+//          in that order, src/knntable.cpp:40-49),
+//   order = std::sort of 0..len-1 by row distance (unstable introsort),
+//   dedup = keep order[j] unless the index at order[j] equals the index at
+//           order[j-1], where both are read from the row while it is being
+//           overwritten with the kept entries (src/knntable.cpp:85-93).
+// Here:
+//   1. count_targets / scan: in-degree of every row and bucket offsets;
+//   2. scatter_incoming: each table entry e = s*k + j appends e to its
+//      target's bucket (atomic cursor; arrival order is not deterministic);
+//   3. merge_rows, one thread per row: sorts its bucket by e, which restores
+//      the one-thread arrival order, builds the row's (distance, position)
+//      items, runs the libstdc++-equivalent introsort (introsort.cuh) and the
+//      in-place deduplication; rows of up to kCap items live in shared
+//      memory, longer rows in a row-aligned global scratch;
+//   4. scan of the kept counts -> row_ptr; compact_rows writes cols, vals and
+//      the source row of every entry (the build_edges pairs).
+#include <algorithm>
+
+#include "common.cuh"
+#include "introsort.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+namespace {
+
+constexpr int kCap = 64;         // row items held in shared memory per thread
+constexpr int kMergeThreads = 128;
+
+// Flags any index outside [0, N) (the table must name existing points).
+__global__ void check_indices(const int32_t *__restrict__ inds, int64_t nk, int64_t N,
+                              int *__restrict__ bad) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t t = inds[e];
+        if (t < 0 || t >= N) atomicOr(bad, 1);
+    }
+}
+
+__global__ void count_targets(const int32_t *__restrict__ inds, int64_t nk,
+                              int32_t *__restrict__ indeg) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk;
+         e += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&indeg[inds[e]], 1);
+}
+
+__global__ void scatter_incoming(const int32_t *__restrict__ inds, int64_t nk,
+                                 const int64_t *__restrict__ in_off, int32_t *__restrict__ cursor,
+                                 int32_t *__restrict__ in_key) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t t = inds[e];
+        const int32_t slot = atomicAdd(&cursor[t], 1);
+        in_key[in_off[t] + slot] = (int32_t)e;
+    }
+}
+
+// Ascending sort of distinct integers (a row's incoming entry ids).
+__device__ void sort_distinct(int32_t *a, int n) {
+    if (n <= 32) {
+        for (int i = 1; i < n; ++i) {
+            int32_t v = a[i];
+            int j = i - 1;
+            while (j >= 0 && a[j] > v) {
+                a[j + 1] = a[j];
+                --j;
+            }
+            a[j + 1] = v;
+        }
+        return;
+    }
+    // heap sort
+    for (int start = n / 2 - 1; start >= 0; --start) {
+        int root = start;
+        for (;;) {
+            int child = 2 * root + 1;
+            if (child >= n) break;
+            if (child + 1 < n && a[child] < a[child + 1]) ++child;
+            if (a[root] >= a[child]) break;
+            int32_t t = a[root];
+            a[root] = a[child];
+            a[child] = t;
+            root = child;
+        }
+    }
+    for (int end = n - 1; end > 0; --end) {
+        int32_t t = a[0];
+        a[0] = a[end];
+        a[end] = t;
+        int root = 0;
+        for (;;) {
+            int child = 2 * root + 1;
+            if (child >= end) break;
+            if (child + 1 < end && a[child] < a[child + 1]) ++child;
+            if (a[root] >= a[child]) break;
+            int32_t u = a[root];
+            a[root] = a[child];
+            a[child] = u;
+            root = child;
+        }
+    }
+}
+
+template <class V>
+__device__ __forceinline__ int32_t merge_one(V items, int L, int k, const int32_t *__restrict__ own_i,
+                                             const float *__restrict__ own_d,
+                                             const int32_t *__restrict__ ink,
+                                             const float *__restrict__ dists, int32_t *out_col,
+                                             float *out_val) {
+    for (int p = 0; p < k; ++p) items[p] = SortItem{own_d[p], p};
+    for (int p = k; p < L; ++p) items[p] = SortItem{dists[ink[p - k]], p};
+    libstdcxx_sort(items, L);
+    // Index stored at row position p before the dedup loop touched it.
+    auto orig = [&](int p) -> int32_t { return p < k ? own_i[p] : ink[p - k] / k; };
+    int32_t n_out = 0;
+    for (int j = 0; j < L; ++j) {
+        const SortItem cur = items[j];
+        bool keep = (j == 0);
+        if (!keep) {
+            const int p = cur.pos, q = items[j - 1].pos;
+            const int32_t vp = p < n_out ? out_col[p] : orig(p);
+            const int32_t vq = q < n_out ? out_col[q] : orig(q);
+            keep = (vp != vq);
+        }
+        if (keep) {
+            out_col[n_out] = orig(cur.pos);
+            out_val[n_out] = cur.key;
+            ++n_out;
+        }
+    }
+    return n_out;
+}
+
+__global__ void __launch_bounds__(kMergeThreads) merge_rows(
+    int64_t N, int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
+    const int64_t *__restrict__ in_off, int32_t *__restrict__ in_key, SortItem *__restrict__ g_items,
+    int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept) {
+    extern __shared__ __align__(16) SortItem sm_items[];  // [kCap][kMergeThreads]
+    const int64_t i = (int64_t)blockIdx.x * kMergeThreads + threadIdx.x;
+    if (i >= N) return;
+    const int64_t ib = in_off[i];
+    const int nin = (int)(in_off[i + 1] - ib);
+    const int L = k + nin;
+    const int64_t base = i * k + ib;  // row-aligned scratch offset
+    int32_t *ink = in_key + ib;
+    sort_distinct(ink, nin);
+    int32_t n;
+    if (L <= kCap) {
+        StridedItems view{sm_items + threadIdx.x, kMergeThreads};
+        n = merge_one(view, L, k, inds + i * k, dists + i * k, ink, dists, out_col + base,
+                      out_val + base);
+    } else {
+        n = merge_one(g_items + base, L, k, inds + i * k, dists + i * k, ink, dists,
+                      out_col + base, out_val + base);
+    }
+    kept[i] = n;
+}
+
+__global__ void compact_rows(int64_t N, int k, const int64_t *__restrict__ in_off,
+                             const int32_t *__restrict__ kept, const int64_t *__restrict__ row_ptr,
+                             const int32_t *__restrict__ out_col, const float *__restrict__ out_val,
+                             int32_t *__restrict__ cols, float *__restrict__ vals,
+                             int32_t *__restrict__ src) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= N) return;
+    const int64_t from = i * k + in_off[i];
+    const int64_t to = row_ptr[i];
+    const int n = kept[i];
+    for (int j = lane; j < n; j += 32) {
+        cols[to + j] = out_col[from + j];
+        vals[to + j] = out_val[from + j];
+        if (src) src[to + j] = (int32_t)i;
+    }
+}
+
+struct SymWs {
+    int32_t *indeg, *cursor, *in_key, *out_col, *kept, *bad;
+    int64_t *in_off;
+    SortItem *items;
+    float *out_val;
+    void *scan;
+};
+
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+SymWs carve(void *ws, int64_t N, int k) {
+    char *p = (char *)ws;
+    SymWs w;
+    const int64_t nk = N * k;
+    w.indeg = (int32_t *)p;    p += align256(sizeof(int32_t) * N);
+    w.cursor = (int32_t *)p;   p += align256(sizeof(int32_t) * N);
+    w.kept = (int32_t *)p;     p += align256(sizeof(int32_t) * N);
+    w.bad = (int32_t *)p;      p += align256(sizeof(int32_t));
+    w.in_off = (int64_t *)p;   p += align256(sizeof(int64_t) * (N + 1));
+    w.in_key = (int32_t *)p;   p += align256(sizeof(int32_t) * nk);
+    w.items = (SortItem *)p;   p += align256(sizeof(SortItem) * 2 * nk);
+    w.out_col = (int32_t *)p;  p += align256(sizeof(int32_t) * 2 * nk);
+    w.out_val = (float *)p;    p += align256(sizeof(float) * 2 * nk);
+    w.scan = p;
+    return w;
+}
+
+}  // namespace
+
+bool indices_in_range(const int32_t *a, int64_t n, int64_t N, cudaStream_t s) {
+    if (n == 0) return true;
+    int *bad = nullptr;
+    NCVIS_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), s));
+    NCVIS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 16 * num_sms());
+    NCVIS_LAUNCH(check_indices, grid, 256, 0, s, a, n, N, bad);
+    int h = 0;
+    NCVIS_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaFreeAsync(bad, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    return h == 0;
+}
+
+size_t symmetrize_workspace_bytes(int64_t N, int k) {
+    const int64_t nk = N * k;
+    return 3 * align256(sizeof(int32_t) * N) + align256(sizeof(int32_t)) +
+           align256(sizeof(int64_t) * (N + 1)) +
+           align256(sizeof(int32_t) * nk) + align256(sizeof(SortItem) * 2 * nk) +
+           align256(sizeof(int32_t) * 2 * nk) + align256(sizeof(float) * 2 * nk) +
+           align256(scan_workspace_bytes(N));
+}
+
+int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists, void *workspace,
+                       int64_t *row_ptr, int32_t *cols, float *vals, int32_t *src,
+                       cudaStream_t s) {
+    require(N >= 1 && k >= 1, "symmetrize: empty table");
+    require(N * (int64_t)k < (int64_t(1) << 30), "symmetrize: N * k must be below 2^30");
+    SymWs w = carve(workspace, N, k);
+    const int64_t nk = N * k;
+    const unsigned grid = (unsigned)std::min<int64_t>((nk + 255) / 256, 16 * num_sms());
+    NCVIS_CUDA(cudaMemsetAsync(w.bad, 0, sizeof(int32_t), s));
+    NCVIS_LAUNCH(check_indices, grid, 256, 0, s, inds, nk, N, w.bad);
+    int bad = 0;
+    NCVIS_CUDA(cudaMemcpyAsync(&bad, w.bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    require(bad == 0, "symmetrize: the kNN table holds an index outside [0, N)");
+    NCVIS_CUDA(cudaMemsetAsync(w.indeg, 0, sizeof(int32_t) * N, s));
+    NCVIS_CUDA(cudaMemsetAsync(w.cursor, 0, sizeof(int32_t) * N, s));
+    NCVIS_LAUNCH(count_targets, grid, 256, 0, s, inds, nk, w.indeg);
+    launch_exclusive_scan_i32_to_i64(w.indeg, w.in_off, N, w.scan, s);
+    NCVIS_LAUNCH(scatter_incoming, grid, 256, 0, s, inds, nk, w.in_off, w.cursor, w.in_key);
+    const size_t smem = sizeof(SortItem) * kCap * kMergeThreads;
+    static bool configured = false;
+    if (!configured) {
+        NCVIS_CUDA(cudaFuncSetAttribute(merge_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        configured = true;
+    }
+    NCVIS_LAUNCH(merge_rows, ceil_div(N, kMergeThreads), kMergeThreads, smem, s, N, k, inds, dists,
+                 w.in_off, w.in_key, w.items, w.out_col, w.out_val, w.kept);
+    launch_exclusive_scan_i32_to_i64(w.kept, row_ptr, N, w.scan, s);
+    NCVIS_LAUNCH(compact_rows, ceil_div(N, 8), 256, 0, s, N, k, w.in_off, w.kept, row_ptr,
+                 w.out_col, w.out_val, cols, vals, src);
+    int64_t E = 0;
+    NCVIS_CUDA(cudaMemcpyAsync(&E, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    return E;
+}
+
+}  // namespace ncvis_gpu

@@ -1,0 +1,133 @@
+"""K7 SGD on the GPU (src/ncvis.cpp:275-352).
+
+Replay mode is held to the reference's one-thread optimizer step by step: a
+step is a block of at most 1024 consecutive edges of one epoch (every
+positive sample and its noise samples), started from the oracle's Y and
+running Q copy; after the step Y and Q must agree to 1e-5 relative
+(|dY| <= 1e-5 * max(1, max|Y|), |dQ| <= 1e-5 * max(1, |Q|)).  The only
+arithmetic difference left is the power/exponential, evaluated in double and
+rounded once on the GPU but by glibc's powf/expf in the reference.
+
+Hogwild mode has no sample-by-sample counterpart (neither has the
+reference's multi-thread run); it is checked for invariants here and for
+embedding quality end to end in test_gpu_fit_transform.py."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+A, B = 0.76687364, 1.22256382
+
+
+def _t(cuda, a, dtype):
+    return cuda.tensor(np.ascontiguousarray(a).astype(dtype), device="cuda")
+
+
+def test_replay_steps_match_oracle(cuda, oracle):
+    from ncvis_gb300 import stages
+    g = golden("embedding.npz")
+    rp, cols, plan = g["rp"], g["cols"], g["plan"]
+    N = rp.size - 1
+    src = oracle.edges_from_csr(rp)
+    E = src.size
+    stream = oracle.negative_stream(N, src, 42, plan)
+    d_src, d_dst = _t(cuda, src, np.int32), _t(cuda, cols, np.int32)
+    d_stream = _t(cuda, stream, np.int32)
+    Y, Q = g["init_d2_e20"].copy(), 0.0
+    pos = 0
+    block = 1024
+    worst_y = worst_q = 0.0
+    for ep in range(plan.size):
+        nu = int(plan[ep])
+        Qc = Q
+        for e0 in range(0, E, block):
+            e1 = min(E, e0 + block)
+            Yn, Qn, pos_n = oracle.optimize_block(Y, Qc, src, cols, ep, plan.size, nu, e0, e1,
+                                                  stream, pos, A, B)
+            dY = _t(cuda, Y, np.float32)
+            dQ = cuda.tensor([Qc], dtype=cuda.float32, device="cuda")
+            stages.optimize_replay(dY, dQ, d_src, d_dst, d_stream, pos, ep, plan.size, nu, A, B,
+                                   edge_begin=e0, edge_end=e1)
+            gy, gq = dY.cpu().numpy(), float(dQ.cpu()[0])
+            ey = np.abs(gy - Yn).max() / max(1.0, np.abs(Yn).max())
+            eq = abs(gq - Qn) / max(1.0, abs(Qn))
+            worst_y, worst_q = max(worst_y, ey), max(worst_q, eq)
+            assert ey <= 1e-5, (ep, e0, ey)
+            assert eq <= 1e-5, (ep, e0, eq)
+            Y, Qc, pos = Yn, Qn, pos_n
+        Q = Qc  # one chain: the epoch average is its own copy
+    print(f"replay worst step error: Y {worst_y:.2e}, Q {worst_q:.2e}")
+
+
+def test_replay_full_epochs_run(cuda, oracle):
+    """Whole epochs chained on the GPU stay finite and close in scale to the
+    reference (the chaotic dynamics make late epochs diverge bitwise)."""
+    from ncvis_gb300 import stages
+    g = golden("embedding.npz")
+    rp, cols, plan = g["rp"], g["cols"], g["plan"]
+    N = rp.size - 1
+    src = oracle.edges_from_csr(rp)
+    stream = oracle.negative_stream(N, src, 42, plan)
+    dY = _t(cuda, g["init_d2_e20"], np.float32)
+    dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+    d_src, d_dst, d_stream = _t(cuda, src, np.int32), _t(cuda, cols, np.int32), _t(cuda, stream, np.int32)
+    pos = 0
+    for ep in range(plan.size):
+        stages.optimize_replay(dY, dQ, d_src, d_dst, d_stream, pos, ep, plan.size, int(plan[ep]), A, B)
+        pos += src.size * int(plan[ep])
+    Y = dY.cpu().numpy()
+    ref = g["opt_d2_Y"]
+    assert np.isfinite(Y).all()
+    assert 0.5 < np.std(Y) / np.std(ref) < 2.0
+    assert abs(float(dQ.cpu()[0]) - float(g["opt_d2_Q"])) < 1.0
+
+
+def test_replay_rejects_bad_stream(cuda, oracle):
+    from ncvis_gb300 import NcvisError, stages
+    g = golden("embedding.npz")
+    rp, cols = g["rp"], g["cols"]
+    N = rp.size - 1
+    src = oracle.edges_from_csr(rp)
+    stream = np.full(src.size * 2, N + 5, np.int32)  # out of range
+    dY = _t(cuda, g["init_d2_e20"], np.float32)
+    before = dY.clone()
+    dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+    with pytest.raises(NcvisError, match="outside"):
+        stages.optimize_replay(dY, dQ, _t(cuda, src, np.int32), _t(cuda, cols, np.int32),
+                               _t(cuda, stream, np.int32), 0, 0, 1, 2, A, B)
+    # the first edge's positive sample ran, the bad noise index stopped the chain
+    assert np.isfinite(dY.cpu().numpy()).all()
+    assert not cuda.isnan(before).any()
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 5])
+def test_hogwild_invariants(cuda, oracle, d):
+    from ncvis_gb300 import stages
+    g = golden("embedding.npz")
+    rp, cols, plan = g["rp"], g["cols"], g["plan"]
+    N = rp.size - 1
+    src = oracle.edges_from_csr(rp)
+    Y0 = oracle.init_embedding(N, d, src, cols, 42, 20, np.float32(1 / 15), 1)
+    dY = _t(cuda, Y0, np.float32)
+    dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+    stages.optimize(dY, dQ, _t(cuda, src, np.int32), _t(cuda, cols, np.int32), 42, plan, A, B,
+                    chains=64)
+    Y = dY.cpu().numpy()
+    assert np.isfinite(Y).all() and np.isfinite(float(dQ.cpu()[0]))
+    # The reference's Q settles near the same value for the same graph.
+    Yr, Qr = oracle.optimize(Y0, 0.0, src, cols, 42, plan, A, B, n_threads=4)
+    assert abs(float(dQ.cpu()[0]) - Qr) < 1.5
+    # Embedding spreads like the reference's.
+    assert 0.5 < np.std(Y) / np.std(Yr) < 2.0
+
+
+def test_hogwild_rejects_bad_edges(cuda):
+    from ncvis_gb300 import NcvisError, stages
+    dY = cuda.zeros((10, 2), dtype=cuda.float32, device="cuda")
+    dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+    src = cuda.tensor([0, 1, 2], dtype=cuda.int32, device="cuda")
+    dst = cuda.tensor([1, 2, 10], dtype=cuda.int32, device="cuda")
+    with pytest.raises(NcvisError, match="outside"):
+        stages.optimize(dY, dQ, src, dst, 1, np.array([1], np.uintp), A, B)
