@@ -108,7 +108,7 @@ class ClockSampler:
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        seen = sorted({n for _, _, flags in rows for n, f in zip(names, flags) if "Active" in f})
+        seen = sorted({n for _, _, flags in rows for n, f in zip(names, flags) if f == "Active"})
         return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
                 "reasons": seen, "samples": len(rows)}
 

@@ -173,6 +173,28 @@ int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const
                                  int n_epochs, size_t n_noise_epoch, float a, float b, float alpha,
                                  float alpha_Q, void *stream);
 
+/* Noise-contrastive loss of a batch of E edges (src[e], dst[e]) with n_noise
+ * uniform noise samples each, drawn from the counter-based stream keyed by
+ * (seed, tag) and counted by the global edge index edge_offset + e; the
+ * objective whose per-sample gradient NCVis::optimize follows
+ * (src/ncvis.cpp:304-323).  *d_loss (device double) = the summed loss. */
+int ncvis_nce_loss_device(size_t N, size_t d, size_t E, const int32_t *d_src, const int32_t *d_dst,
+                          const float *dY, const float *dQ, size_t n_noise, float a, float b,
+                          uint64_t seed, uint32_t tag, uint64_t edge_offset, double *d_loss,
+                          void *stream);
+
+/* Gradient of the same loss scaled by *d_scale (device float): d_gradY [N, d]
+ * is accumulated into (+=), *d_gradQ (device double) is written. */
+int ncvis_nce_grad_device(size_t N, size_t d, size_t E, const int32_t *d_src, const int32_t *d_dst,
+                          const float *dY, const float *dQ, size_t n_noise, float a, float b,
+                          uint64_t seed, uint32_t tag, uint64_t edge_offset, const float *d_scale,
+                          float *d_gradY, double *d_gradQ, void *stream);
+
+/* The noise indices the loss uses for edges [0, E): out [E, n_noise] (device
+ * int32), for checking the loss against an independent implementation. */
+int ncvis_nce_noise_device(size_t N, size_t E, const int32_t *d_src, size_t n_noise, uint64_t seed,
+                           uint32_t tag, uint64_t edge_offset, int32_t *d_out, void *stream);
+
 /* Number of kernels this library has launched in the process so far. */
 uint64_t ncvis_kernel_launch_count(void);
 

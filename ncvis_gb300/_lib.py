@@ -110,6 +110,13 @@ SIGNATURES = {
     "ncvis_optimize_replay_device": (C.c_int, [_sz, _sz, _vp, _vp, _sz, _sz, _vp, _sz, _vp, _vp,
                                                C.c_int, C.c_int, _sz, C.c_float, C.c_float,
                                                C.c_float, C.c_float, _vp]),
+    "ncvis_nce_loss_device": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, _sz, C.c_float,
+                                        C.c_float, C.c_uint64, C.c_uint32, C.c_uint64, _vp, _vp]),
+    "ncvis_nce_grad_device": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, _sz, C.c_float,
+                                        C.c_float, C.c_uint64, C.c_uint32, C.c_uint64, _vp, _vp,
+                                        _vp, _vp]),
+    "ncvis_nce_noise_device": (C.c_int, [_sz, _sz, _vp, _sz, C.c_uint64, C.c_uint32, C.c_uint64,
+                                         _vp, _vp]),
     "ncvis_kernel_launch_count": (C.c_uint64, []),
     "ncvis_version": (C.c_char_p, []),
 }

@@ -154,15 +154,17 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const int d = (int)p.d;
     const int dist = p.distance;
     const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
-    require(!bf16, "[ncvis] the BF16 tensor-core kNN is not available in this build",
-            kUnsupported);
     require((int64_t)N * k < (int64_t(1) << 30), "[ncvis] N * n_neighbors must be below 2^30");
     require(host || ((uintptr_t)Y & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
     const bool replay = (o.sgd_mode == NCVIS_SGD_REPLAY);
 
     cudaStream_t s = stream();
     KnnPlan kp = plan_knn_f32((int64_t)N, k, o.rerank_factor);
-    const int C = kp.C();
+    KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, k, o.rerank_factor);
+    if (bf16)
+        require(knn_tc_supported((int)D, tp.R),
+                "[ncvis] the BF16 tensor-core kNN supports D <= 128", kUnsupported);
+    const int C = bf16 ? tp.R : kp.C();
     const int64_t nk = (int64_t)N * k;
     const int chains = o.sgd_chains > 0 ? o.sgd_chains : sgd_default_chains(2 * nk);
 
@@ -172,6 +174,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const size_t o_Xp = L.take(sizeof(float) * N * D);
     const size_t o_sqn = L.take(sizeof(float) * N);
     const size_t o_flag = L.take(sizeof(int) * 4);
+    const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
     const size_t o_ci = L.take(sizeof(int32_t) * N * C);
     const size_t o_cd = L.take(sizeof(float) * N * C);
     const size_t o_ki = L.take(sizeof(int32_t) * nk);
@@ -192,6 +195,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     float *Xp = (float *)(base + o_Xp);
     float *sqn = (float *)(base + o_sqn);
     int *flag = (int *)(base + o_flag);
+    __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
     int32_t *cand_i = (int32_t *)(base + o_ci);
     float *cand_d = (float *)(base + o_cd);
     int32_t *knn_i = (int32_t *)(base + o_ki);
@@ -208,7 +212,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         NCVIS_CUDA(cudaMemcpyAsync((void *)dX, X, sizeof(float) * N * D, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
-    launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, nullptr, 0, flag, s);
+    launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
     {
         int bad = 0;
@@ -217,10 +221,20 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
-    launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
+    if (bf16)
+        launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s);
+    else
+        launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
     launch_rerank(Xp, (int64_t)N, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
+    if (bf16) {
+        int timeout = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(timeout == 0, "[ncvis] the tensor-core kNN kernel timed out waiting on a barrier",
+                kDeviceTimeout);
+    }
     const int64_t E = run_symmetrize((int64_t)N, k, knn_i, knn_d, base + o_sym, row_ptr, cols, vals,
                                      src, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[5], s));
@@ -357,22 +371,30 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
         require(D >= 1 && N < (size_t(1) << 31) && N * k < (size_t(1) << 30),
                 "knn: need D >= 1, N < 2^31 and N * k < 2^30");
         require(distance >= 0 && distance <= 3, "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
-        require(precision == NCVIS_KNN_FP32, "knn: the BF16 tensor-core kNN is not available in this build",
-                kUnsupported);
+        require(precision == NCVIS_KNN_FP32 || precision == NCVIS_KNN_BF16_RERANK,
+                "knn: unknown precision mode");
+        const bool bf16 = (precision == NCVIS_KNN_BF16_RERANK);
         cudaStream_t s = (cudaStream_t)stream;
         KnnPlan kp = plan_knn_f32((int64_t)N, (int)k, rerank_factor);
-        const int C = kp.C();
+        KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, (int)k, rerank_factor);
+        if (bf16)
+            require(knn_tc_supported((int)D, tp.R),
+                    "knn: the BF16 tensor-core kNN supports D <= 128", kUnsupported);
+        const int C = bf16 ? tp.R : kp.C();
         Layout L;
         const size_t o_Xp = L.take(sizeof(float) * N * D);
         const size_t o_sqn = L.take(sizeof(float) * N);
-        const size_t o_flag = L.take(sizeof(int));
+        const size_t o_flag = L.take(sizeof(int) * 2);
         const size_t o_ci = L.take(sizeof(int32_t) * N * C);
         const size_t o_cd = L.take(sizeof(float) * N * C);
+        const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
         char *base = nullptr;
         NCVIS_CUDA(cudaMallocAsync((void **)&base, L.total, s));
-        NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int), s));
+        NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int) * 2, s));
+        __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
         launch_preprocess(dX, (int64_t)N, (int)D, distance, (float *)(base + o_Xp),
-                          (float *)(base + o_sqn), nullptr, 0, (int *)(base + o_flag), s);
+                          (float *)(base + o_sqn), Xb, bf16 ? tp.ldb : 0, (int *)(base + o_flag),
+                          s);
         int bad = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&bad, base + o_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
@@ -381,8 +403,23 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
             throw Error(kInvalidArgument, "knn: input contains non-finite values");
         }
         NCVIS_CUDA(cudaMemsetAsync(d_inds, 0xff, sizeof(int32_t) * N * k, s));
-        launch_knn_select_f32((float *)(base + o_Xp), (float *)(base + o_sqn), (int64_t)N, (int)D,
-                              distance, kp, (int32_t *)(base + o_ci), (float *)(base + o_cd), s);
+        if (bf16) {
+            launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
+                                 (int32_t *)(base + o_ci), (float *)(base + o_cd),
+                                 (int *)(base + o_flag) + 1, s);
+            int timeout = 0;
+            NCVIS_CUDA(cudaMemcpyAsync(&timeout, (int *)(base + o_flag) + 1, sizeof(int),
+                                       cudaMemcpyDeviceToHost, s));
+            NCVIS_CUDA(cudaStreamSynchronize(s));
+            if (timeout) {
+                cudaFreeAsync(base, s);
+                throw Error(kDeviceTimeout, "knn: the tensor-core kernel timed out waiting on a barrier");
+            }
+        } else {
+            launch_knn_select_f32((float *)(base + o_Xp), (float *)(base + o_sqn), (int64_t)N,
+                                  (int)D, distance, kp, (int32_t *)(base + o_ci),
+                                  (float *)(base + o_cd), s);
+        }
         launch_rerank((float *)(base + o_Xp), (int64_t)N, (int)D, distance,
                       (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s);
         NCVIS_CUDA(cudaFreeAsync(base, s));
@@ -488,6 +525,62 @@ int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const
         NCVIS_CUDA(cudaFreeAsync(err, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(herr == 0, "optimize_replay: an index outside [0, N) was met; replay stopped");
+    });
+}
+
+int ncvis_nce_loss_device(size_t N, size_t d, size_t E, const int32_t *d_src, const int32_t *d_dst,
+                          const float *dY, const float *dQ, size_t n_noise, float a, float b,
+                          uint64_t seed, uint32_t tag, uint64_t edge_offset, double *d_loss,
+                          void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_dst && dY && dQ && d_loss, "nce_loss: null pointer");
+        require(N >= 2 && N < (size_t(1) << 31) && d >= 1 && d <= 32 && n_noise >= 1 &&
+                    n_noise <= 1024,
+                "nce_loss: need 2 <= N < 2^31, 1 <= d <= 32, 1 <= n_noise <= 1024");
+        cudaStream_t s = (cudaStream_t)stream;
+        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
+                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+                "nce_loss: an edge endpoint is outside [0, N)");
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));
+        run_nce(0, (int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, (int)n_noise, a, b, seed,
+                tag, edge_offset, nullptr, nullptr, d_loss, ws, s);
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+    });
+}
+
+int ncvis_nce_grad_device(size_t N, size_t d, size_t E, const int32_t *d_src, const int32_t *d_dst,
+                          const float *dY, const float *dQ, size_t n_noise, float a, float b,
+                          uint64_t seed, uint32_t tag, uint64_t edge_offset, const float *d_scale,
+                          float *d_gradY, double *d_gradQ, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_dst && dY && dQ && d_scale && d_gradY && d_gradQ,
+                "nce_grad: null pointer");
+        require(N >= 2 && N < (size_t(1) << 31) && d >= 1 && d <= 32 && n_noise >= 1 &&
+                    n_noise <= 1024,
+                "nce_grad: need 2 <= N < 2^31, 1 <= d <= 32, 1 <= n_noise <= 1024");
+        cudaStream_t s = (cudaStream_t)stream;
+        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
+                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+                "nce_grad: an edge endpoint is outside [0, N)");
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));
+        run_nce(1, (int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, (int)n_noise, a, b, seed,
+                tag, edge_offset, d_scale, d_gradY, d_gradQ, ws, s);
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+    });
+}
+
+int ncvis_nce_noise_device(size_t N, size_t E, const int32_t *d_src, size_t n_noise, uint64_t seed,
+                           uint32_t tag, uint64_t edge_offset, int32_t *d_out, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_out, "nce_noise: null pointer");
+        require(N >= 2 && N < (size_t(1) << 31), "nce_noise: need 2 <= N < 2^31");
+        cudaStream_t s = (cudaStream_t)stream;
+        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s),
+                "nce_noise: a source is outside [0, N)");
+        launch_noise_table((int64_t)N, (int64_t)E, d_src, (int)n_noise, seed, tag, edge_offset,
+                           d_out, s);
     });
 }
 

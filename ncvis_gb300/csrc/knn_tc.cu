@@ -1,0 +1,461 @@
+// K2: kNN candidate selection on the 5th-generation tensor cores (tcgen05),
+// BF16 operands with FP32 accumulation; the candidates are re-ranked exactly
+// in FP32 afterwards (K4, knn_simt.cu), which restores the reference's
+// distances (src/ncvis.cpp:72-153) on the selected set.
+//
+// Work decomposition (one persistent CTA per SM, 12 warps):
+//   * a query tile is 256 preprocessed points (two M=128 halves), held in
+//     shared memory for the whole sweep (TMA, 128-byte swizzle, K-major);
+//   * candidate tiles of 128 points stream through a 4-stage TMA ring;
+//   * warp 0 issues TMA, warp 1 allocates TMEM and issues tcgen05.mma
+//     (M=128, N=128, K=16 steps) into one of two double-buffered 2x128-column
+//     FP32 accumulators (512 TMEM columns);
+//   * warps 4..11 own one query row each (TMEM lane = row): they read the
+//     accumulator with tcgen05.ld, turn dot products into ranking scores
+//     (-<q,c> for the inner-product spaces, |c|^2 - 2<q,c> for squared L2),
+//     and keep the R best candidates of their row in a list in global memory
+//     (a running worst-score threshold filters whole 32-column chunks, so
+//     list updates are rare after the first tiles).
+// Every mbarrier wait is bounded in time: on expiry the CTA sets *err,
+// stops, drains its MMAs and in-flight TMA copies, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <string>
+
+#include "common.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+namespace {
+
+constexpr int kQueryTile = 256;   // queries per CTA tile (2 x M=128)
+constexpr int kCandTile = 128;    // candidates per tile (N=128)
+constexpr int kStages = 4;        // candidate-tile ring
+constexpr int kAtomBytes = 128 * 128;  // 128 rows x 128 bytes (64 bf16) per swizzle atom column
+constexpr int kMaxAtoms = 2;      // K <= 128
+constexpr int kThreads = 384;
+constexpr int kEpiWarp0 = 4;
+constexpr int kEpiWarps = 8;
+constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+struct SharedStorage {
+    // 1024-byte aligned tiles first (128B swizzle atoms repeat every 1024 B).
+    uint8_t a[2][kMaxAtoms][kAtomBytes];
+    uint8_t b[kStages][kMaxAtoms][kAtomBytes];
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t a_full, a_empty;
+    uint64_t acc_full[2], acc_empty[2];
+    uint64_t drain;
+    uint32_t tmem_base;
+    volatile int abort;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of `parity`; false if it expired or the CTA aborted.
+__device__ __forceinline__ bool mbar_wait(SharedStorage &s, uint64_t *bar, uint32_t parity,
+                                          int *err, int code) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (s.abort) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            s.abort = 1;
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
+                                            int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused with 128B swizzle, K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // version
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D f32, A and B bf16, both K-major, M=128, N=128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kCandTile >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(acc), "r"(kIdesc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// A row's candidate list: R (score, index) pairs in global memory, unsorted,
+// with the worst pair tracked in registers once the list is full.
+struct RowList {
+    float *sc;
+    int32_t *ix;
+    int R, n, worst_pos;
+    float worst;
+};
+
+__device__ __noinline__ void list_insert(RowList &L, float score, int32_t idx) {
+    int p;
+    if (L.n < L.R) {
+        p = L.n++;
+    } else {
+        p = L.worst_pos;
+    }
+    L.sc[p] = score;
+    L.ix[p] = idx;
+    if (L.n == L.R) {
+        float w = -FLT_MAX;
+        int wp = 0;
+        for (int t = 0; t < L.R; ++t) {
+            const float v = L.sc[t];
+            if (v > w) {
+                w = v;
+                wp = t;
+            }
+        }
+        L.worst = w;
+        L.worst_pos = wp;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    knn_select_tc(const __grid_constant__ CUtensorMap tmap, const float *__restrict__ sqnorm,
+                  int64_t N, int ksteps, int katoms, int dist, int R, int32_t *__restrict__ cand_i,
+                  float *__restrict__ cand_s, int *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    SharedStorage &s = *reinterpret_cast<SharedStorage *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
+    const int64_t n_ct = (N + kCandTile - 1) / kCandTile;
+    const uint32_t a_bytes = 2u * katoms * kAtomBytes;
+    const uint32_t b_bytes = (uint32_t)katoms * kAtomBytes;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            mbar_init(&s.full[i], 1);
+            mbar_init(&s.empty[i], 1);
+        }
+        mbar_init(&s.a_full, 1);
+        mbar_init(&s.a_empty, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&s.acc_full[i], 1);
+            mbar_init(&s.acc_empty[i], kEpiWarps);
+        }
+        mbar_init(&s.drain, 1);
+        s.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&s.tmem_base)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tmem = s.tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------------------------------------------------- TMA producer
+        int stage = 0;
+        uint32_t phase = 0, a_phase = 0;
+        uint32_t issued_parity[kStages];
+        bool issued[kStages];
+        for (int i = 0; i < kStages; ++i) issued[i] = false, issued_parity[i] = 0;
+        bool a_issued = false;
+        uint32_t a_parity = 0;
+        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
+            if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1)) break;
+            mbar_expect_tx(&s.a_full, a_bytes);
+            for (int h = 0; h < 2; ++h)
+                for (int at = 0; at < katoms; ++at)
+                    tma_load_2d(s.a[h][at], &tmap, &s.a_full, at * 64,
+                                (int)(qt * kQueryTile + h * 128));
+            a_issued = true;
+            a_parity = a_phase;
+            a_phase ^= 1;
+            for (int64_t ct = 0; ct < n_ct; ++ct) {
+                if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2)) break;
+                mbar_expect_tx(&s.full[stage], b_bytes);
+                for (int at = 0; at < katoms; ++at)
+                    tma_load_2d(s.b[stage][at], &tmap, &s.full[stage], at * 64,
+                                (int)(ct * kCandTile));
+                issued[stage] = true;
+                issued_parity[stage] = phase;
+                if (++stage == kStages) stage = 0, phase ^= 1;
+            }
+        }
+        // Copies still in flight must land before the CTA's shared memory goes away.
+        const long long t0 = clock64();
+        for (int i = 0; i < kStages; ++i)
+            if (issued[i])
+                while (!mbar_try_wait(&s.full[i], issued_parity[i]) && clock64() - t0 < kWaitCycles) {
+                }
+        if (a_issued)
+            while (!mbar_try_wait(&s.a_full, a_parity) && clock64() - t0 < kWaitCycles) {
+            }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------------------------------------------------- MMA issuer
+        int stage = 0;
+        uint32_t phase = 0, a_phase = 0, acc_phase = 0;
+        int acc = 0;
+        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
+            if (!mbar_wait(s, &s.a_full, a_phase, err, 3)) break;
+            a_phase ^= 1;
+            tmem_fence_after();
+            for (int64_t ct = 0; ct < n_ct; ++ct) {
+                if (!mbar_wait(s, &s.acc_empty[acc], acc_phase ^ 1, err, 4)) break;
+                if (!mbar_wait(s, &s.full[stage], phase, err, 5)) break;
+                tmem_fence_after();
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t d_tmem = tmem + (uint32_t)(acc * 256 + h * 128);
+                    for (int ks = 0; ks < ksteps; ++ks) {
+                        const int at = ks >> 2;
+                        const uint32_t off = (uint32_t)(ks & 3) * 32;
+                        const uint64_t ad = smem_desc(smem_u32(s.a[h][at]) + off);
+                        const uint64_t bd = smem_desc(smem_u32(s.b[stage][at]) + off);
+                        umma_bf16(d_tmem, ad, bd, ks > 0 ? 1u : 0u);
+                    }
+                }
+                umma_commit(&s.empty[stage]);
+                umma_commit(&s.acc_full[acc]);
+                if (++stage == kStages) stage = 0, phase ^= 1;
+                acc ^= 1;
+                if (acc == 0) acc_phase ^= 1;
+            }
+            umma_commit(&s.a_empty);
+        }
+        // Every issued MMA completes before TMEM is released.
+        umma_commit(&s.drain);
+        const long long t0 = clock64();
+        while (!mbar_try_wait(&s.drain, 0) && clock64() - t0 < kWaitCycles) {
+        }
+    } else if (warp >= kEpiWarp0) {
+        // ---------------------------------------------------------- epilogue
+        const int h = (warp - kEpiWarp0) >> 2;
+        const int quad = warp & 3;
+        const int row_in_tile = h * 128 + quad * 32 + lane;
+        const bool l2 = (dist == kSquaredL2);
+        uint32_t acc_phase = 0;
+        int acc = 0;
+        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
+            const int64_t grow = qt * kQueryTile + row_in_tile;
+            const bool live = grow < N;
+            RowList L;
+            L.R = R;
+            L.n = 0;
+            L.worst_pos = 0;
+            L.worst = FLT_MAX;
+            L.sc = cand_s + (live ? grow : 0) * R;
+            L.ix = cand_i + (live ? grow : 0) * R;
+            bool ok = true;
+            for (int64_t ct = 0; ct < n_ct; ++ct) {
+                if (!mbar_wait(s, &s.acc_full[acc], acc_phase, err, 6)) {
+                    ok = false;
+                    break;
+                }
+                tmem_fence_after();
+                const int64_t c0 = ct * kCandTile;
+                const bool tail = c0 + kCandTile > N;
+#pragma unroll 1
+                for (int chunk = 0; chunk < kCandTile / 32; ++chunk) {
+                    float v[32];
+                    __syncwarp();
+                    const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
+                                           (uint32_t)(acc * 256 + h * 128 + chunk * 32);
+                    tmem_ld32(taddr, v);
+                    tmem_wait_ld();
+                    const int64_t cb = c0 + chunk * 32;
+                    float best = FLT_MAX;
+                    if (l2) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int64_t c = cb + j;
+                            const float nc = (c < N) ? __ldg(sqnorm + c) : 0.f;
+                            v[j] = fmaf(-2.f, v[j], nc);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) v[j] = -v[j];
+                    }
+                    if (tail) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (cb + j >= N) v[j] = FLT_MAX;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) best = fminf(best, v[j]);
+                    if (live && best < L.worst) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (v[j] < L.worst) list_insert(L, v[j], (int32_t)(cb + j));
+                    }
+                }
+                tmem_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&s.acc_empty[acc]);
+                acc ^= 1;
+                if (acc == 0) acc_phase ^= 1;
+            }
+            if (!ok) break;
+            if (live)
+                for (int p = L.n; p < R; ++p) {
+                    L.ix[p] = -1;
+                    L.sc[p] = FLT_MAX;
+                }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tmem_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols));
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        NCVIS_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                    cudaEnableDefault, &q));
+        require(q == cudaDriverEntryPointSuccess && p != nullptr,
+                "knn: cuTensorMapEncodeTiled is unavailable", kCudaError);
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+}  // namespace
+
+KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor) {
+    KnnTcPlan p;
+    if (rerank_factor <= 0) rerank_factor = 4;
+    int64_t R = std::max<int64_t>((int64_t)rerank_factor * k, (int64_t)k + 1);
+    p.R = (int)std::min<int64_t>(R, N);
+    p.ldb = (D + 7) / 8 * 8;
+    p.Npad = N;
+    return p;
+}
+
+bool knn_tc_supported(int D, int R) { return D >= 1 && D <= 64 * kMaxAtoms && R <= 1024; }
+
+void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
+                          const KnnTcPlan &plan, int dist, int32_t *cand_i, float *cand_d,
+                          int *timeout_flag, cudaStream_t s) {
+    require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
+    const int ksteps = (plan.ldb + 15) / 16;
+    const int katoms = (ksteps * 16 + 63) / 64;
+    require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
+    require(((uintptr_t)Xb & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
+    CUtensorMap map;
+    cuuint64_t dims[2] = {(cuuint64_t)plan.ldb, (cuuint64_t)N};
+    cuuint64_t strides[1] = {(cuuint64_t)plan.ldb * 2};
+    cuuint32_t box[2] = {64, 128};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)Xb, dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    require(r == CUDA_SUCCESS, "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")",
+            kCudaError);
+    const size_t smem = sizeof(SharedStorage) + 1024;
+    static bool configured = false;
+    if (!configured) {
+        NCVIS_CUDA(cudaFuncSetAttribute(knn_select_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        configured = true;
+    }
+    const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
+    const unsigned grid = (unsigned)std::min<int64_t>(n_qt, num_sms());
+    NCVIS_LAUNCH(knn_select_tc, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms, dist,
+                 plan.R, cand_i, cand_d, timeout_flag);
+}
+
+}  // namespace ncvis_gpu

@@ -101,10 +101,41 @@ __host__ __device__ inline Philox4x32 philox4x32_10(uint32_t c0, uint32_t c1, ui
     return out;
 }
 
-// Uniform index in [0, n) from 64 random bits (multiply-shift; bias <= n/2^64).
+// Uniform index in [0, n) from 64 random bits r = hi:lo, floor(r * n / 2^64)
+// (multiply-shift; bias <= n/2^64), computed as (hi*n + (lo*n >> 32)) >> 32.
 __host__ __device__ inline uint32_t bounded_index(uint32_t lo, uint32_t hi, uint32_t n) {
-    uint64_t r = ((uint64_t)hi << 32) | lo;
-    return (uint32_t)(((u128)r * n) >> 64);
+    const uint64_t a = (uint64_t)hi * n;
+    const uint64_t b = ((uint64_t)lo * n) >> 32;
+    return (uint32_t)((a + b) >> 32);
+}
+
+// Noise sample `s` (0-based) of edge `e` with source `i`, stream tag `tag`
+// (the epoch for SGD, a caller-chosen tag for the loss): a uniform index in
+// [0, n) other than i.  Philox4x32-10 block (e_lo, e_hi, tag, s/2) under key
+// (k0, k1) gives two 64-bit draws, used by even and odd s; an index equal to
+// i is redrawn from blocks (e_lo, e_hi ^ retry<<16, tag, s/2 | 2^31) under key
+// (k0 ^ retry, k1), at most 64 times, then replaced by i+1 mod n.
+__host__ __device__ inline uint32_t noise_index(uint32_t k0, uint32_t k1, uint64_t e, uint32_t tag,
+                                                uint32_t s, uint32_t i, uint32_t n) {
+    const Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), tag, s >> 1, k0, k1);
+    const int h = (int)(s & 1);
+    uint32_t o = bounded_index(r.v[2 * h], r.v[2 * h + 1], n);
+    for (uint32_t retry = 1; o == i; ++retry) {
+        if (retry > 64) {
+            o = (o + 1 == n) ? 0 : o + 1;
+            break;
+        }
+        const Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16), tag,
+                                            (s >> 1) | 0x80000000u, k0 ^ retry, k1);
+        o = bounded_index(rr.v[0], rr.v[1], n);
+    }
+    return o;
+}
+
+// Key words of a 64-bit seed.
+__host__ __device__ inline void noise_key(uint64_t seed, uint32_t &k0, uint32_t &k1) {
+    k0 = (uint32_t)seed;
+    k1 = (uint32_t)(seed >> 32) ^ 0x5eed1u;
 }
 
 }  // namespace ncvis_gpu

@@ -123,9 +123,9 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                                                       uint32_t N, const float *__restrict__ Q_in,
                                                       double *__restrict__ q_part, EpochConst k,
                                                       int epoch, uint32_t key0, uint32_t key1,
-                                                      int64_t chunk) {
+                                                      int64_t chunk, int64_t n_chains) {
     const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-    const int64_t e0 = chain * chunk;
+    const int64_t e0 = chain < n_chains ? chain * chunk : E;
     const int64_t e1 = min(E, e0 + chunk);
     float Qc = *Q_in;
     for (int64_t e = e0; e < e1; ++e) {
@@ -145,34 +145,18 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                 yi.v[c] = (yi.v[c] + dx) - dx;
             }
         }
-        for (int s = 0; s < k.nu; s += 2) {
-            uint32_t retry = 0;
-            Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)epoch,
-                                         (uint32_t)(s >> 1), key0, key1);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (s + h >= k.nu) break;
-                uint32_t o = bounded_index(r.v[2 * h], r.v[2 * h + 1], N);
-                while (o == (uint32_t)i) {  // redraw, as the reference does
-                    if (++retry > 64) {  // P = N^-64: never in practice; keeps the loop finite
-                        o = (o + 1 == N) ? 0 : o + 1;
-                        break;
-                    }
-                    Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16),
-                                                  (uint32_t)epoch, (uint32_t)(s >> 1) | 0x80000000u,
-                                                  key0 ^ retry, key1);
-                    o = bounded_index(rr.v[0], rr.v[1], N);
-                }
-                Vec<D> yo = load_row<D>(Y, o);
-                apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), false, k, Qc));
-                store_row<D>(Y, o, yo);
-            }
+        for (int s = 0; s < k.nu; ++s) {
+            const uint32_t o = noise_index(key0, key1, (uint64_t)e, (uint32_t)epoch, (uint32_t)s,
+                                           (uint32_t)i, N);
+            Vec<D> yo = load_row<D>(Y, o);
+            apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), false, k, Qc));
+            store_row<D>(Y, o, yo);
         }
         store_row<D>(Y, i, yi);
     }
     // Chain copies of Q, summed in FP64 per block.
     __shared__ double red[kThreads / 32];
-    double v = Qc;
+    double v = chain < n_chains ? (double)Qc : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -188,34 +172,18 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
 __global__ void __launch_bounds__(kThreads) sgd_epoch_generic(
     float *__restrict__ Y, int d, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
     int64_t E, uint32_t N, const float *__restrict__ Q_in, double *__restrict__ q_part, EpochConst k,
-    int epoch, uint32_t key0, uint32_t key1, int64_t chunk) {
+    int epoch, uint32_t key0, uint32_t key1, int64_t chunk, int64_t n_chains) {
     const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-    const int64_t e0 = chain * chunk;
+    const int64_t e0 = chain < n_chains ? chain * chunk : E;
     const int64_t e1 = min(E, e0 + chunk);
     float Qc = *Q_in;
     for (int64_t e = e0; e < e1; ++e) {
         const int64_t i = src[e];
         for (int s = 0; s <= k.nu; ++s) {
-            int64_t o;
-            if (s == 0) {
-                o = dst[e];
-            } else {
-                const int sn = s - 1;
-                Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)epoch,
-                                             (uint32_t)(sn >> 1), key0, key1);
-                o = bounded_index(r.v[2 * (sn & 1)], r.v[2 * (sn & 1) + 1], N);
-                uint32_t retry = 0;
-                while (o == i) {
-                    if (++retry > 64) {
-                        o = (o + 1 == (int64_t)N) ? 0 : o + 1;
-                        break;
-                    }
-                    Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16),
-                                                  (uint32_t)epoch, (uint32_t)(sn >> 1) | 0x80000000u,
-                                                  key0 ^ retry, key1);
-                    o = bounded_index(rr.v[0], rr.v[1], N);
-                }
-            }
+            const int64_t o = (s == 0) ? (int64_t)dst[e]
+                                       : (int64_t)noise_index(key0, key1, (uint64_t)e,
+                                                              (uint32_t)epoch, (uint32_t)(s - 1),
+                                                              (uint32_t)i, N);
             float d2 = 0.f;
             for (int c = 0; c < d; ++c) {
                 const float t = __ldcg(Y + i * d + c) - __ldcg(Y + o * d + c);
@@ -230,7 +198,7 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch_generic(
         }
     }
     __shared__ double red[kThreads / 32];
-    double v = Qc;
+    double v = chain < n_chains ? (double)Qc : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -379,33 +347,34 @@ void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const siz
     require(g.N >= 2 && g.N < (int64_t(1) << 31), "optimize: N must be in [2, 2^31)");
     if (chains <= 0) chains = sgd_default_chains(g.E);
     const int blocks = (int)ceil_div(chains, kThreads);
-    const int64_t total_chains = (int64_t)blocks * kThreads;
+    const int64_t total_chains = chains;
     const int64_t chunk = (g.E + total_chains - 1) / total_chains;
     double *q_part = (double *)workspace;
-    const uint32_t key0 = (uint32_t)g.seed, key1 = (uint32_t)(g.seed >> 32) ^ 0x5eed1u;
+    uint32_t key0, key1;
+    noise_key(g.seed, key0, key1);
     for (int ep = epoch_begin; ep < epoch_end; ++ep) {
         const int nu = (int)n_noise[ep];
         EpochConst k = epoch_const(g, ep, nu);
         switch (g.d) {
             case 1:
                 NCVIS_LAUNCH(sgd_epoch<1>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
-                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
                 break;
             case 2:
                 NCVIS_LAUNCH(sgd_epoch<2>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
-                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
                 break;
             case 3:
                 NCVIS_LAUNCH(sgd_epoch<3>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
-                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
                 break;
             case 4:
                 NCVIS_LAUNCH(sgd_epoch<4>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.E,
-                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                             (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
                 break;
             default:
                 NCVIS_LAUNCH(sgd_epoch_generic, blocks, kThreads, 0, s, g.Y, g.d, g.src, g.dst,
-                             g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk);
+                             g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
         }
         NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, blocks, total_chains, g.Q);
     }

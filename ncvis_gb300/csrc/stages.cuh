@@ -90,4 +90,16 @@ void launch_sgd_replay(const SgdArgs &args, int epoch, size_t nu, int64_t edge_b
                        int64_t edge_end, const int32_t *stream, int64_t stream_offset, int *err,
                        cudaStream_t s);
 
+// ---- K8 NCE loss (the objective of src/ncvis.cpp:275-352) --------------------
+size_t nce_workspace_bytes(int64_t E);
+// mode 0: *out = loss (FP64 sum); mode 1: dY += (*scale) dL/dY (atomic FP32),
+// *out = (*scale) dL/dQ (FP64).
+void run_nce(int mode, int64_t N, int d, int64_t E, const int32_t *src, const int32_t *dst,
+             const float *Y, const float *Q, int nu, float a, float b, uint64_t seed,
+             uint32_t tag, uint64_t edge_offset, const float *scale, float *dY, double *out,
+             void *workspace, cudaStream_t s);
+// The loss's noise indices for edges [0, E): out [E, nu].
+void launch_noise_table(int64_t N, int64_t E, const int32_t *src, int nu, uint64_t seed,
+                        uint32_t tag, uint64_t edge_offset, int32_t *out, cudaStream_t s);
+
 }  // namespace ncvis_gpu

@@ -113,11 +113,11 @@ def test_hogwild_invariants(cuda, oracle, d):
     dY = _t(cuda, Y0, np.float32)
     dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
     stages.optimize(dY, dQ, _t(cuda, src, np.int32), _t(cuda, cols, np.int32), 42, plan, A, B,
-                    chains=64)
+                    chains=8)
     Y = dY.cpu().numpy()
     assert np.isfinite(Y).all() and np.isfinite(float(dQ.cpu()[0]))
-    # The reference's Q settles near the same value for the same graph.
-    Yr, Qr = oracle.optimize(Y0, 0.0, src, cols, 42, plan, A, B, n_threads=4)
+    # The reference (8 threads = 8 chains) settles Q near the same value.
+    Yr, Qr = oracle.optimize(Y0, 0.0, src, cols, 42, plan, A, B, n_threads=8)
     assert abs(float(dQ.cpu()[0]) - Qr) < 1.5
     # Embedding spreads like the reference's.
     assert 0.5 < np.std(Y) / np.std(Yr) < 2.0
