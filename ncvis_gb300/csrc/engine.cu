@@ -166,7 +166,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
                 "[ncvis] the BF16 tensor-core kNN supports D <= 128", kUnsupported);
     const int C = bf16 ? tp.R : kp.C();
     const int64_t nk = (int64_t)N * k;
-    const int chains = o.sgd_chains > 0 ? o.sgd_chains : sgd_default_chains(2 * nk);
+    const int chains = o.sgd_chains > 0 ? o.sgd_chains : 0;  // 0: sized once E is known
 
     Layout L;
     const size_t o_X = host ? L.take(sizeof(float) * N * D) : 0;
@@ -492,7 +492,7 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
         require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
                     indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
                 "optimize: an edge endpoint is outside [0, N)");
-        if (chains <= 0) chains = sgd_default_chains((int64_t)E);
+        if (chains <= 0) chains = sgd_default_chains((int64_t)E, (int)d);
         void *ws = nullptr;
         NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
         SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,

@@ -132,6 +132,18 @@ __host__ __device__ inline uint32_t noise_index(uint32_t k0, uint32_t k1, uint64
     return o;
 }
 
+// Noise samples 2p and 2p+1 of edge e: the same indices as noise_index for
+// those s, from one Philox block.
+__host__ __device__ inline void noise_pair(uint32_t k0, uint32_t k1, uint64_t e, uint32_t tag,
+                                           uint32_t p, uint32_t i, uint32_t n, uint32_t &o0,
+                                           uint32_t &o1) {
+    const Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), tag, p, k0, k1);
+    o0 = bounded_index(r.v[0], r.v[1], n);
+    o1 = bounded_index(r.v[2], r.v[3], n);
+    if (o0 == i) o0 = noise_index(k0, k1, e, tag, 2 * p, i, n);
+    if (o1 == i) o1 = noise_index(k0, k1, e, tag, 2 * p + 1, i, n);
+}
+
 // Key words of a 64-bit seed.
 __host__ __device__ inline void noise_key(uint64_t seed, uint32_t &k0, uint32_t &k1) {
     k0 = (uint32_t)seed;

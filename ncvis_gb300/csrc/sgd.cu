@@ -84,9 +84,10 @@ __device__ __forceinline__ float nce_weight(float d2, bool positive, const Epoch
         p1 = k.pow_b1_at_zero;
     }
     const float denom = fmaf(k.a, p, 1.f);
-    const float ph = __frcp_rn(denom);
+    const float ph = __fdividef(1.f, denom);
     const float nm = k.nu_f * __expf(Qc);
-    float w = positive ? __frcp_rn(__fdividef(ph, nm) + 1.f) : -__frcp_rn(fmaf(nm, denom, 1.f));
+    float w = positive ? __fdividef(1.f, __fdividef(ph, nm) + 1.f)
+                       : -__fdividef(1.f, fmaf(nm, denom, 1.f));
     Qc = fmaf(-w, k.alpha_Q, Qc);
     w = w * p1 * (2.f * k.ab * ph);
     return w * k.step;
@@ -116,6 +117,27 @@ __device__ __forceinline__ void apply(Vec<D> &yi, Vec<D> &yo, float ws) {
     }
 }
 
+// Samples of a group whose row was loaded before an earlier sample of the
+// same group stored it are reloaded, so a chain always sees its own updates.
+template <int D, int G>
+__device__ __forceinline__ void run_group(float *Y, Vec<D> &yi, const uint32_t (&o)[G], int count,
+                                          bool first_is_positive, const EpochConst &k, float &Qc) {
+    Vec<D> yo[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t)
+        if (t < count) yo[t] = load_row<D>(Y, o[t]);
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+        if (t >= count) break;
+        bool dup = false;
+#pragma unroll
+        for (int u = 0; u < t; ++u) dup |= (o[u] == o[t]);
+        if (dup) yo[t] = load_row<D>(Y, o[t]);
+        apply<D>(yi, yo[t], nce_weight(sq_dist<D>(yi, yo[t]), first_is_positive && t == 0, k, Qc));
+        store_row<D>(Y, o[t], yo[t]);
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                                                       const int32_t *__restrict__ src,
@@ -128,14 +150,19 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
     const int64_t e0 = chain < n_chains ? chain * chunk : E;
     const int64_t e1 = min(E, e0 + chunk);
     float Qc = *Q_in;
+    const uint32_t tag = (uint32_t)epoch;
     for (int64_t e = e0; e < e1; ++e) {
-        const int32_t i = src[e];
-        const int32_t j = dst[e];
+        const uint32_t i = (uint32_t)src[e];
+        const uint32_t j = (uint32_t)dst[e];
         Vec<D> yi = load_row<D>(Y, i);
+        int s = 0;  // next noise sample
         if (j != i) {
-            Vec<D> yo = load_row<D>(Y, j);
-            apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), true, k, Qc));
-            store_row<D>(Y, j, yo);
+            // The positive sample and the first noise pair share one group.
+            uint32_t o[3] = {j, 0u, 0u};
+            const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
+            if (k.nu >= 1) noise_pair(key0, key1, (uint64_t)e, tag, 0, i, N, o[1], o[2]);
+            run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
+            s = cnt - 1;
         } else {
             // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
             const float ws = nce_weight(0.f, true, k, Qc);
@@ -145,12 +172,12 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                 yi.v[c] = (yi.v[c] + dx) - dx;
             }
         }
-        for (int s = 0; s < k.nu; ++s) {
-            const uint32_t o = noise_index(key0, key1, (uint64_t)e, (uint32_t)epoch, (uint32_t)s,
-                                           (uint32_t)i, N);
-            Vec<D> yo = load_row<D>(Y, o);
-            apply<D>(yi, yo, nce_weight(sq_dist<D>(yi, yo), false, k, Qc));
-            store_row<D>(Y, o, yo);
+        // Remaining noise samples in groups of four (two Philox blocks each).
+        for (; s < k.nu; s += 4) {
+            uint32_t o[4];
+            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), i, N, o[0], o[1]);
+            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, i, N, o[2], o[3]);
+            run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
         }
         store_row<D>(Y, i, yi);
     }
@@ -330,22 +357,42 @@ EpochConst epoch_const(const SgdArgs &g, int epoch, int nu) {
 
 }  // namespace
 
-int sgd_default_chains(int64_t E) {
-    // Enough chains to fill the GPU, but at least ~64 edges each so that a
-    // chain's Q copy follows many samples before the epoch average.
-    int64_t chains = (int64_t)num_sms() * 1024;
-    chains = std::min<int64_t>(chains, std::max<int64_t>(E / 64, 1));
+namespace {
+
+// Threads of the d-specialised epoch kernel that fit on the GPU at once.
+int64_t resident_chains(int d) {
+    int blocks = 0;
+    cudaError_t err;
+    switch (d) {
+        case 1: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch<1>, kThreads, 0); break;
+        case 2: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch<2>, kThreads, 0); break;
+        case 3: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch<3>, kThreads, 0); break;
+        case 4: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch<4>, kThreads, 0); break;
+        default:
+            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch_generic, kThreads, 0);
+    }
+    if (err != cudaSuccess || blocks < 1) blocks = 1;
+    return (int64_t)blocks * kThreads * num_sms();
+}
+
+}  // namespace
+
+int sgd_default_chains(int64_t E, int d) {
+    // Every chain resident at once, each with at least ~64 edges so that its
+    // copy of Q follows many samples before the epoch average.
+    int64_t chains = std::min<int64_t>(resident_chains(d), std::max<int64_t>(E / 64, 1));
     return (int)std::max<int64_t>(chains, 1);
 }
 
 size_t sgd_workspace_bytes(int chains) {
-    return sizeof(double) * ((chains + kThreads - 1) / kThreads + 1);
+    const int64_t most = std::max<int64_t>(chains, (int64_t)num_sms() * 2048);
+    return sizeof(double) * ((most + kThreads - 1) / kThreads + 1);
 }
 
 void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s) {
     require(g.N >= 2 && g.N < (int64_t(1) << 31), "optimize: N must be in [2, 2^31)");
-    if (chains <= 0) chains = sgd_default_chains(g.E);
+    if (chains <= 0) chains = sgd_default_chains(g.E, g.d);
     const int blocks = (int)ceil_div(chains, kThreads);
     const int64_t total_chains = chains;
     const int64_t chunk = (g.E + total_chains - 1) / total_chains;

@@ -82,7 +82,7 @@ struct SgdArgs {
     float a, b, alpha, alpha_Q;
 };
 size_t sgd_workspace_bytes(int chains);
-int sgd_default_chains(int64_t E);
+int sgd_default_chains(int64_t E, int d);
 void run_sgd_hogwild(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s);
 // *err (device int) is set to 1 if an index outside [0, N) is met.
