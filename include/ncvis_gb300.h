@@ -120,6 +120,18 @@ int ncvis_fit_transform(ncvis_handle h, const float *X, size_t N, size_t D, floa
  * after the work is enqueued and the edge count is known. */
 int ncvis_fit_transform_device(ncvis_handle h, const float *dX, size_t N, size_t D, float *dY);
 
+/* Many independent embeddings in one run.  Problem p is rows
+ * [offsets[p], offsets[p+1]) of dX [offsets[n], D] (device) and gets rows of
+ * dY [offsets[n], d] (device); offsets (n+1 entries) and seeds (n entries,
+ * NULL: every problem uses random_seed) are host arrays.  Every problem
+ * follows the engine's parameters (k clamped by the smallest problem) with
+ * its own kNN graph, initialisation stream, noise range and Q; the SGD epoch
+ * loop of all problems runs as one captured CUDA graph.  FP32 kNN, d <= 4.
+ * No reference counterpart (the reference embeds one dataset per call). */
+int ncvis_fit_transform_batched_device(ncvis_handle h, const float *dX, size_t D,
+                                       const int64_t *offsets, size_t n_problems,
+                                       const uint64_t *seeds, float *dY);
+
 const char *ncvis_last_error(ncvis_handle h);
 const char *ncvis_get_last_error(void);
 int ncvis_get_stage_times(ncvis_handle h, ncvis_stage_times *out);

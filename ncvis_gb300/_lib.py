@@ -96,6 +96,7 @@ SIGNATURES = {
     "ncvis_set_options": (C.c_int, [_vp, C.POINTER(NcvisOptions)]),
     "ncvis_fit_transform": (C.c_int, [_vp, _vp, _sz, _sz, _vp]),
     "ncvis_fit_transform_device": (C.c_int, [_vp, _vp, _sz, _sz, _vp]),
+    "ncvis_fit_transform_batched_device": (C.c_int, [_vp, _vp, _sz, _vp, _sz, _vp, _vp]),
     "ncvis_last_error": (C.c_char_p, [_vp]),
     "ncvis_get_last_error": (C.c_char_p, []),
     "ncvis_get_stage_times": (C.c_int, [_vp, C.POINTER(NcvisStageTimes)]),

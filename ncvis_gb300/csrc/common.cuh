@@ -54,6 +54,9 @@ std::atomic<uint64_t> &launch_counter();
         NCVIS_CUDA(cudaGetLastError());                                              \
     } while (0)
 
+// Makes `msg` the text ncvis_get_last_error() returns on this thread.
+void record_error(const char *msg);
+
 inline int num_sms() {
     static int sms = [] {
         int dev = 0, v = 0;
@@ -65,5 +68,21 @@ inline int num_sms() {
 }
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+#ifdef __CUDACC__
+// Index of the segment holding `t` in an ascending prefix array p[0..B]
+// (p[0] <= t < p[B]).
+__device__ __forceinline__ int segment_of(const int64_t *__restrict__ p, int B, int64_t t) {
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p[mid] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+#endif
 
 }  // namespace ncvis_gpu

@@ -6,7 +6,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -56,6 +59,72 @@ struct Events {
 
 }  // namespace
 
+void record_error(const char *msg) { g_last_error = msg; }
+
+// Picks, per problem signature, the fastest of a few candidate settings by
+// timing one run of each with CUDA events; results are cached per engine and,
+// when NCVIS_AUTOTUNE_CACHE names a file, kept there as "key value" lines.
+struct Autotuner {
+    std::map<std::string, int> best;
+    bool loaded = false;
+
+    static const char *cache_path() { return std::getenv("NCVIS_AUTOTUNE_CACHE"); }
+
+    void load() {
+        loaded = true;
+        const char *path = cache_path();
+        if (!path) return;
+        std::ifstream in(path);
+        std::string key;
+        int value;
+        while (in >> key >> value) best[key] = value;
+    }
+
+    void save() const {
+        const char *path = cache_path();
+        if (!path) return;
+        std::ofstream out(path);
+        for (const auto &kv : best) out << kv.first << " " << kv.second << "\n";
+    }
+
+    template <class Run>
+    int pick(const std::string &key, const std::vector<int> &candidates, Run run, cudaStream_t s) {
+        if (!loaded) load();
+        auto it = best.find(key);
+        if (it != best.end()) return it->second;
+        cudaEvent_t a, b;
+        NCVIS_CUDA(cudaEventCreate(&a));
+        NCVIS_CUDA(cudaEventCreate(&b));
+        int choice = candidates.front();
+        float best_ms = 1e30f;
+        for (int c : candidates) {
+            NCVIS_CUDA(cudaEventRecord(a, s));
+            run(c);
+            NCVIS_CUDA(cudaEventRecord(b, s));
+            NCVIS_CUDA(cudaEventSynchronize(b));
+            float ms = 0.f;
+            NCVIS_CUDA(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best_ms) best_ms = ms, choice = c;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        best[key] = choice;
+        save();
+        return choice;
+    }
+};
+
+namespace {
+
+// eoff[p] = row_ptr[off[p]] for p in [0, B].
+__global__ void gather_offsets(const int64_t *__restrict__ row_ptr,
+                               const int64_t *__restrict__ off, int B, int64_t *__restrict__ eoff) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p <= B) eoff[p] = row_ptr[off[p]];
+}
+
+}  // namespace
+
 }  // namespace ncvis_gpu
 
 using namespace ncvis_gpu;
@@ -100,6 +169,9 @@ struct ncvis_engine {
     }
 
     void fit(const float *X, size_t N, size_t D, float *Y, bool host);
+    void fit_batched(const float *dX, size_t D, const int64_t *offsets, size_t B,
+                     const uint64_t *seeds, float *dY);
+    Autotuner tuner;
 };
 
 namespace {
@@ -301,6 +373,229 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     times.k = k;
 }
 
+void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets, size_t B,
+                               const uint64_t *seeds, float *dY) {
+    require(dX && dY && offsets && B >= 1, "[ncvis] batched: null pointer or no problems");
+    require(B < (size_t(1) << 20), "[ncvis] batched: too many problems");
+    require(offsets[0] == 0, "[ncvis] batched: offsets[0] must be 0");
+    int64_t min_n = INT64_MAX;
+    for (size_t p = 0; p < B; ++p) {
+        const int64_t n = offsets[p + 1] - offsets[p];
+        require(n >= 2, "[ncvis] batched: every problem needs at least two points");
+        min_n = std::min(min_n, n);
+    }
+    const int64_t total = offsets[B];
+    require(D >= 1 && total < (int64_t(1) << 31), "[ncvis] batched: need D >= 1 and total N < 2^31");
+    require(p.distance >= 0 && p.distance <= 3,
+            "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
+    require(p.d >= 1 && p.d <= 4, "[ncvis] batched: embedding dimension d must be in [1, 4]");
+    require(o.knn_precision == NCVIS_KNN_FP32, "[ncvis] batched: FP32 kNN only", kUnsupported);
+    require(((uintptr_t)dY & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
+    // k is clamped by the smallest problem (src/ncvis.cpp:381-382 per problem).
+    int64_t kk = std::min<int64_t>((int64_t)p.n_neighbors, min_n - 1);
+    kk = std::max<int64_t>(kk, 1);
+    require(kk <= 255, "[ncvis] n_neighbors above 255 is not supported");
+    const int k = (int)kk, d = (int)p.d, dist = p.distance;
+    const int64_t nk = total * k;
+    require(nk < (int64_t(1) << 30), "[ncvis] batched: total N * n_neighbors must be below 2^30");
+    cudaStream_t s = stream();
+
+    // Host-side layout of the problems.
+    const int qt = knn_f32_query_tile(), it = init_tile_rows();
+    std::vector<int64_t> h_off(offsets, offsets + B + 1), h_tq(B + 1), h_ti(B + 1);
+    std::vector<uint64_t> h_seed(B);
+    h_tq[0] = h_ti[0] = 0;
+    for (size_t q = 0; q < B; ++q) {
+        const int64_t n = h_off[q + 1] - h_off[q];
+        h_tq[q + 1] = h_tq[q] + (n + qt - 1) / qt;
+        h_ti[q + 1] = h_ti[q] + (n + it - 1) / it;
+        h_seed[q] = seeds ? seeds[q] : (uint64_t)p.random_seed;
+    }
+    KnnPlan kp;
+    kp.R = (int)std::min<int64_t>(std::min<int64_t>(
+        std::max<int64_t>((int64_t)(o.rerank_factor > 0 ? o.rerank_factor : 2) * k, k + 1), min_n), 256);
+    kp.splits = 1;
+    while (h_tq[B] * kp.splits < 2 * num_sms() && kp.splits * 2 * kp.R <= 1024 &&
+           min_n / (kp.splits * 2) >= 64)
+        kp.splits *= 2;
+    const int C = kp.C();
+    const int64_t max_chains = std::max<int64_t>(sgd_batched_resident_chains(d), (int64_t)B);
+
+    Layout L;
+    const size_t o_Xp = L.take(sizeof(float) * total * D);
+    const size_t o_sqn = L.take(sizeof(float) * total);
+    const size_t o_flag = L.take(sizeof(int) * 4);
+    const size_t o_ci = L.take(sizeof(int32_t) * total * C);
+    const size_t o_cd = L.take(sizeof(float) * total * C);
+    const size_t o_ki = L.take(sizeof(int32_t) * nk);
+    const size_t o_kd = L.take(sizeof(float) * nk);
+    const size_t o_rp = L.take(sizeof(int64_t) * (total + 1));
+    const size_t o_cols = L.take(sizeof(int32_t) * 2 * nk);
+    const size_t o_vals = L.take(sizeof(float) * 2 * nk);
+    const size_t o_src = L.take(sizeof(int32_t) * 2 * nk);
+    const size_t o_sym = L.take(symmetrize_workspace_bytes(total, k));
+    const size_t o_init = L.take(init_batched_workspace_bytes(total, h_ti[B], (int)B, d));
+    const size_t o_off = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_tq = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_ti = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_eoff = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_cp = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_seed = L.take(sizeof(uint64_t) * B);
+    const size_t o_Qs = L.take(sizeof(float) * B);
+    const size_t o_cq = L.take(sizeof(float) * max_chains);
+    const size_t o_Yt = L.take(sizeof(float) * total * d);
+    const size_t o_Qt = L.take(sizeof(float) * B);
+    char *base = ensure_arena(L.total);
+    float *Xp = (float *)(base + o_Xp);
+    float *sqn = (float *)(base + o_sqn);
+    int *flag = (int *)(base + o_flag);
+    int32_t *cand_i = (int32_t *)(base + o_ci);
+    float *cand_d = (float *)(base + o_cd);
+    int32_t *knn_i = (int32_t *)(base + o_ki);
+    float *knn_d = (float *)(base + o_kd);
+    int64_t *row_ptr = (int64_t *)(base + o_rp);
+    int32_t *cols = (int32_t *)(base + o_cols);
+    float *vals = (float *)(base + o_vals);
+    int32_t *src = (int32_t *)(base + o_src);
+    int64_t *d_off = (int64_t *)(base + o_off), *d_tq = (int64_t *)(base + o_tq);
+    int64_t *d_ti = (int64_t *)(base + o_ti), *d_eoff = (int64_t *)(base + o_eoff);
+    int64_t *d_cp = (int64_t *)(base + o_cp);
+    uint64_t *d_seed = (uint64_t *)(base + o_seed);
+    float *Qs = (float *)(base + o_Qs), *chain_q = (float *)(base + o_cq);
+    float *Ytune = (float *)(base + o_Yt), *Qtune = (float *)(base + o_Qt);
+
+    Events ev;
+    NCVIS_CUDA(cudaEventRecord(ev.ev[0], s));
+    NCVIS_CUDA(cudaMemcpyAsync(d_off, h_off.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaMemcpyAsync(d_tq, h_tq.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaMemcpyAsync(d_ti, h_ti.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaMemcpyAsync(d_seed, h_seed.data(), sizeof(uint64_t) * B, cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
+    NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
+    launch_preprocess(dX, total, (int)D, dist, Xp, sqn, nullptr, 0, flag, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
+    {
+        int bad = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(bad == 0, "[ncvis] input contains non-finite values");
+    }
+    NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
+    Segments seg;
+    seg.offsets = d_off;
+    seg.tile_prefix = d_tq;
+    seg.B = (int)B;
+    seg.n_tiles = h_tq[B];
+    launch_knn_select_f32(Xp, sqn, total, (int)D, dist, kp, cand_i, cand_d, s, seg);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
+    launch_rerank(Xp, total, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
+    const int64_t E = run_symmetrize(total, k, knn_i, knn_d, base + o_sym, row_ptr, cols, vals, src, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[5], s));
+
+    // Edge ranges per problem, then chains per problem in proportion to edges.
+    NCVIS_LAUNCH(gather_offsets, ceil_div(B + 1, 256), 256, 0, s, row_ptr, d_off, (int)B, d_eoff);
+    std::vector<int64_t> h_eoff(B + 1);
+    NCVIS_CUDA(cudaMemcpyAsync(h_eoff.data(), d_eoff, sizeof(int64_t) * (B + 1),
+                               cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    auto chain_layout = [&](int edges_per_chain, std::vector<int64_t> &cp) {
+        const int64_t target = std::min<int64_t>(max_chains, std::max<int64_t>(E / edges_per_chain, (int64_t)B));
+        cp.assign(B + 1, 0);
+        for (size_t q = 0; q < B; ++q) {
+            const int64_t Ep = h_eoff[q + 1] - h_eoff[q];
+            int64_t c = (int64_t)((double)target * (double)Ep / (double)std::max<int64_t>(E, 1));
+            c = std::max<int64_t>(1, std::min<int64_t>(c, std::max<int64_t>(Ep / 16, 1)));
+            cp[q + 1] = cp[q] + c;
+        }
+        return cp[B];
+    };
+
+    const float init_alpha = (float)(1. / k);
+    run_init_embedding_batched(total, d, d_off, d_ti, (int)B, h_ti[B], d_seed, row_ptr, cols,
+                               p.n_init_epochs, init_alpha, dY, base + o_init, s);
+    NCVIS_CUDA(cudaEventRecord(ev.ev[6], s));
+
+    SgdBatch g{};
+    g.d = d;
+    g.B = (int)B;
+    g.src = src;
+    g.dst = cols;
+    g.off = d_off;
+    g.eoff = d_eoff;
+    g.cp = d_cp;
+    g.chain_q = chain_q;
+    g.seed = (uint64_t)p.random_seed;
+    g.a = p.a;
+    g.b = p.b;
+    g.alpha = p.alpha;
+    g.alpha_Q = p.alpha_Q;
+    std::vector<int64_t> h_cp;
+    if (p.n_epochs > 0 && E > 0) {
+        // Autotune edges per chain on a scratch copy of the embedding (one epoch each).
+        const std::string key = "sgd_batched d=" + std::to_string(d) + " B=" + std::to_string(B) +
+                                " E~2^" + std::to_string((int)std::log2((double)std::max<int64_t>(E, 1)));
+        const int chosen = tuner.pick(key, {16, 32, 64, 128}, [&](int epc) {
+            g.n_chains = chain_layout(epc, h_cp);
+            NCVIS_CUDA(cudaMemcpyAsync(d_cp, h_cp.data(), sizeof(int64_t) * (B + 1),
+                                       cudaMemcpyHostToDevice, s));
+            NCVIS_CUDA(cudaMemcpyAsync(Ytune, dY, sizeof(float) * total * d, cudaMemcpyDeviceToDevice, s));
+            NCVIS_CUDA(cudaMemsetAsync(Qtune, 0, sizeof(float) * B, s));
+            SgdBatch t = g;
+            t.Y = Ytune;
+            t.Qs = Qtune;
+            t.n_epochs = 1;
+            run_sgd_hogwild_batched(t, noise.data() + (p.n_epochs - 1), s);
+        }, s);
+        g.n_chains = chain_layout(chosen, h_cp);
+        NCVIS_CUDA(cudaMemcpyAsync(d_cp, h_cp.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
+        NCVIS_CUDA(cudaMemsetAsync(Qs, 0, sizeof(float) * B, s));
+        g.Y = dY;
+        g.Qs = Qs;
+        g.n_epochs = p.n_epochs;
+        // The whole epoch loop as one CUDA graph, launched once.
+        cudaStream_t cs;
+        NCVIS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        NCVIS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        try {
+            run_sgd_hogwild_batched(g, noise.data(), cs);
+        } catch (...) {
+            cudaStreamEndCapture(cs, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cudaStreamDestroy(cs);
+            throw;
+        }
+        NCVIS_CUDA(cudaStreamEndCapture(cs, &graph));
+        NCVIS_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        NCVIS_CUDA(cudaEventRecord(ev.ev[9], s));
+        NCVIS_CUDA(cudaGraphLaunch(exec, s));
+        NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
+        NCVIS_CUDA(cudaEventSynchronize(ev.ev[7]));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+    } else {
+        NCVIS_CUDA(cudaEventRecord(ev.ev[9], s));
+        NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
+    }
+    NCVIS_CUDA(cudaEventRecord(ev.ev[8], s));
+    NCVIS_CUDA(cudaEventSynchronize(ev.ev[8]));
+    times.h2d_ms = ev.ms(0, 1);
+    times.preprocess_ms = ev.ms(1, 2);
+    times.knn_ms = ev.ms(2, 3);
+    times.rerank_ms = ev.ms(3, 4);
+    times.symmetrize_ms = ev.ms(4, 5);
+    times.build_edges_ms = 0.f;
+    times.init_ms = ev.ms(5, 6);
+    times.optimize_ms = ev.ms(9, 7);
+    times.d2h_ms = 0.f;
+    times.total_ms = ev.ms(0, 8);
+    times.n_edges = E;
+    times.k = k;
+}
+
 // ------------------------------------------------------------------------ C ABI
 
 extern "C" {
@@ -351,6 +646,13 @@ int ncvis_fit_transform(ncvis_handle h, const float *X, size_t N, size_t D, floa
 int ncvis_fit_transform_device(ncvis_handle h, const float *dX, size_t N, size_t D, float *dY) {
     if (!h) return NCVIS_INVALID_ARGUMENT;
     return guarded(h, [&] { h->fit(dX, N, D, dY, false); });
+}
+
+int ncvis_fit_transform_batched_device(ncvis_handle h, const float *dX, size_t D,
+                                       const int64_t *offsets, size_t n_problems,
+                                       const uint64_t *seeds, float *dY) {
+    if (!h) return NCVIS_INVALID_ARGUMENT;
+    return guarded(h, [&] { h->fit_batched(dX, D, offsets, n_problems, seeds, dY); });
 }
 
 const char *ncvis_last_error(ncvis_handle h) { return h ? h->err.c_str() : "null handle"; }

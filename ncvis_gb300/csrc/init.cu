@@ -121,9 +121,146 @@ __global__ void standardize(int64_t n, int d, float *__restrict__ Y, const float
     }
 }
 
+// ---- batched problems: problem p owns rows [off[p], off[p+1]), its own
+// seed, and row tiles [tp[p], tp[p+1]) of kThreads rows each.
+
+__global__ void uniform_init_batched(float *__restrict__ Y, int64_t total, int d,
+                                     const int64_t *__restrict__ off, int B,
+                                     const uint64_t *__restrict__ seeds) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int p = segment_of(off, B, t / d);
+    Pcg64 g(seeds[p]);
+    g.advance((uint64_t)(t - off[p] * d));
+    Y[t] = unit_float(g.next());
+}
+
+__device__ __forceinline__ int64_t tile_rows(const int64_t *tp, const int64_t *off, int B, int &p,
+                                             int64_t &row_end) {
+    p = segment_of(tp, B, blockIdx.x);
+    row_end = off[p + 1];
+    return off[p] + ((int64_t)blockIdx.x - tp[p]) * kThreads + threadIdx.x;
+}
+
+__global__ void __launch_bounds__(kThreads) spmm_rows_batched(
+    const int64_t *__restrict__ tp, const int64_t *__restrict__ off, int B, int d,
+    const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ cols, float alpha,
+    const float *__restrict__ Yold, float *__restrict__ Ynew, double *__restrict__ part) {
+    int p;
+    int64_t row_end;
+    const int64_t i = tile_rows(tp, off, B, p, row_end);
+    double sums[kMaxDim];
+    for (int c = 0; c < d; ++c) sums[c] = 0;
+    if (i < row_end) {
+        float acc[kMaxDim];
+        for (int c = 0; c < d; ++c) acc[c] = 0.f;
+        const int64_t p1 = row_ptr[i + 1];
+        for (int64_t q = row_ptr[i]; q < p1; ++q) {
+            const float *y = Yold + (int64_t)cols[q] * d;
+            for (int c = 0; c < d; ++c) acc[c] = __fadd_rn(acc[c], __fmul_rn(alpha, y[c]));
+        }
+        for (int c = 0; c < d; ++c) {
+            Ynew[i * d + c] = acc[c];
+            sums[c] = acc[c];
+        }
+    }
+    block_partial(sums, d, part);
+}
+
+__global__ void __launch_bounds__(kThreads) centred_squares_batched(
+    const int64_t *__restrict__ tp, const int64_t *__restrict__ off, int B, int d,
+    const float *__restrict__ Y, const float *__restrict__ mean, double *__restrict__ part) {
+    int p;
+    int64_t row_end;
+    const int64_t i = tile_rows(tp, off, B, p, row_end);
+    double sums[kMaxDim];
+    for (int c = 0; c < d; ++c) {
+        sums[c] = 0;
+        if (i < row_end) {
+            const float dev = __fsub_rn(Y[i * d + c], mean[p * d + c]);
+            sums[c] = __fmul_rn(dev, dev);
+        }
+    }
+    block_partial(sums, d, part);
+}
+
+// One block per problem: stat[p*d + c] from the partials of p's tiles.
+__global__ void finish_stat_batched(const double *__restrict__ part, const int64_t *__restrict__ tp,
+                                    const int64_t *__restrict__ off, int d, int mode,
+                                    float *__restrict__ stat) {
+    __shared__ double red[32];
+    const int p = blockIdx.x;
+    const int64_t n = off[p + 1] - off[p];
+    for (int c = 0; c < d; ++c) {
+        double s = 0;
+        for (int64_t b = tp[p] + threadIdx.x; b < tp[p + 1]; b += blockDim.x) s += part[b * d + c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+            const float v = __fdiv_rn((float)t, (float)n);
+            stat[p * d + c] = (mode == 0) ? v : sqrtf(v);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void standardize_batched(int64_t total, int d, const int64_t *__restrict__ off, int B,
+                                    float *__restrict__ Y, const float *__restrict__ mean,
+                                    const float *__restrict__ sigma) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = t / d;
+        const int c = (int)(t - row * d);
+        const int p = segment_of(off, B, row);
+        Y[t] = __fdiv_rn(__fsub_rn(Y[t], mean[p * d + c]), sigma[p * d + c]);
+    }
+}
+
 inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 }  // namespace
+
+int init_tile_rows() { return kThreads; }
+
+size_t init_batched_workspace_bytes(int64_t total_rows, int64_t n_tiles, int B, int d) {
+    return align256(sizeof(float) * total_rows * d) + align256(sizeof(double) * n_tiles * d) +
+           2 * align256(sizeof(float) * B * d);
+}
+
+void run_init_embedding_batched(int64_t total_rows, int d, const int64_t *off, const int64_t *tp,
+                                int B, int64_t n_tiles, const uint64_t *seeds,
+                                const int64_t *row_ptr, const int32_t *cols, int n_init_epochs,
+                                float alpha, float *Y, void *workspace, cudaStream_t s) {
+    require(d >= 1 && d <= kMaxDim, "init_embedding: d must be in [1, 32]");
+    char *p = (char *)workspace;
+    float *other = (float *)p;   p += align256(sizeof(float) * total_rows * d);
+    double *part = (double *)p;  p += align256(sizeof(double) * n_tiles * d);
+    float *mean = (float *)p;    p += align256(sizeof(float) * B * d);
+    float *sigma = (float *)p;
+    const int64_t n = total_rows * d;
+    NCVIS_LAUNCH(uniform_init_batched, ceil_div(n, kThreads), kThreads, 0, s, Y, n, d, off, B, seeds);
+    float *bufs[2] = {Y, other};
+    const unsigned elem_grid = (unsigned)std::min<int64_t>((n + kThreads - 1) / kThreads,
+                                                           8 * num_sms());
+    for (int ep = 0; ep < n_init_epochs; ++ep) {
+        const float *y_old = bufs[ep % 2];
+        float *y_new = bufs[(ep + 1) % 2];
+        NCVIS_LAUNCH(spmm_rows_batched, (unsigned)n_tiles, kThreads, 0, s, tp, off, B, d, row_ptr,
+                     cols, alpha, y_old, y_new, part);
+        NCVIS_LAUNCH(finish_stat_batched, B, 256, 0, s, part, tp, off, d, 0, mean);
+        NCVIS_LAUNCH(centred_squares_batched, (unsigned)n_tiles, kThreads, 0, s, tp, off, B, d,
+                     y_new, mean, part);
+        NCVIS_LAUNCH(finish_stat_batched, B, 256, 0, s, part, tp, off, d, 1, sigma);
+        NCVIS_LAUNCH(standardize_batched, elem_grid, kThreads, 0, s, n, d, off, B, y_new, mean,
+                     sigma);
+    }
+    if (n_init_epochs % 2)
+        NCVIS_CUDA(cudaMemcpyAsync(Y, other, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+}
 
 size_t init_workspace_bytes(int64_t N, int d) {
     const int64_t blocks = (N + kThreads - 1) / kThreads;

@@ -67,19 +67,30 @@ __device__ inline SelectSmem carve(char *base, int R) {
     return s;
 }
 
+// With seg.B > 0 the points form seg.B independent problems, problem p owning
+// rows [offsets[p], offsets[p+1]) and query tiles [tile_prefix[p],
+// tile_prefix[p+1]); a query only sees candidates of its own problem.
 __global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ Xp,
                                                      const float *__restrict__ sqnorm, int64_t N,
                                                      int D, int dist, int R, int splits,
                                                      int32_t *__restrict__ cand_i,
-                                                     float *__restrict__ cand_d) {
+                                                     float *__restrict__ cand_d, Segments seg) {
     extern __shared__ __align__(16) char smem_raw[];
     SelectSmem sm = carve(smem_raw, R);
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    const int64_t q0 = (int64_t)blockIdx.x * BM;
+    int64_t q0 = (int64_t)blockIdx.x * BM, lo = 0, hi = N;
+    if (seg.B > 0) {
+        const int p = segment_of(seg.tile_prefix, seg.B, blockIdx.x);
+        lo = seg.offsets[p];
+        hi = seg.offsets[p + 1];
+        q0 = lo + ((int64_t)blockIdx.x - seg.tile_prefix[p]) * BM;
+    }
+    const int64_t n_seg = hi - lo;
     const int split = blockIdx.y;
-    const int64_t c_begin = N * split / splits;
-    const int64_t c_end = N * (split + 1) / splits;
+    const int64_t c_begin = lo + n_seg * split / splits;
+    const int64_t c_end = lo + n_seg * (split + 1) / splits;
+    N = hi;  // queries of this tile stop at the end of their problem
     const bool l2 = (dist == kSquaredL2);
 
     if (tid < BM) {
@@ -254,6 +265,8 @@ __global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp,
 
 }  // namespace
 
+int knn_f32_query_tile() { return BM; }
+
 KnnPlan plan_knn_f32(int64_t N, int k, int rerank_factor) {
     KnnPlan p;
     if (rerank_factor <= 0) rerank_factor = 2;
@@ -272,7 +285,8 @@ KnnPlan plan_knn_f32(int64_t N, int k, int rerank_factor) {
 }
 
 void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int D, int dist,
-                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s) {
+                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s,
+                           const Segments &seg) {
     const size_t smem = select_smem_bytes(plan.R);
     static size_t configured = 0;
     if (smem > configured) {
@@ -280,9 +294,10 @@ void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int 
                                         (int)smem));
         configured = smem;
     }
-    dim3 grid(ceil_div(N, BM), plan.splits);
+    const int64_t tiles = seg.B > 0 ? seg.n_tiles : (int64_t)ceil_div(N, BM);
+    dim3 grid((unsigned)tiles, plan.splits);
     NCVIS_LAUNCH(knn_select_f32, grid, NT, smem, s, Xp, sqnorm, N, D, dist, plan.R, plan.splits,
-                 cand_i, cand_d);
+                 cand_i, cand_d, seg);
 }
 
 void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,

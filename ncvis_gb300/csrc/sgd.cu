@@ -237,6 +237,82 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch_generic(
     }
 }
 
+// Batched problems: problem p owns rows [off[p], off[p+1]), edges
+// [eoff[p], eoff[p+1]) and chains [cp[p], cp[p+1]); its noise samples are
+// uniform over its own rows; chain copies of its Q go to chain_q.
+template <int D>
+__global__ void __launch_bounds__(kThreads) sgd_epoch_batched(
+    float *__restrict__ Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
+    const int64_t *__restrict__ off, const int64_t *__restrict__ eoff,
+    const int64_t *__restrict__ cp, int B, int64_t n_chains, const float *__restrict__ Qs,
+    float *__restrict__ chain_q, EpochConst k, int epoch, uint32_t key0, uint32_t key1) {
+    const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (chain >= n_chains) return;
+    const int p = segment_of(cp, B, chain);
+    const int64_t lc = chain - cp[p], nc = cp[p + 1] - cp[p];
+    const int64_t Ep = eoff[p + 1] - eoff[p];
+    const int64_t chunk = (Ep + nc - 1) / nc;
+    const int64_t e0 = eoff[p] + min(Ep, lc * chunk);
+    const int64_t e1 = eoff[p] + min(Ep, (lc + 1) * chunk);
+    const uint32_t base = (uint32_t)off[p];
+    const uint32_t Np = (uint32_t)(off[p + 1] - off[p]);
+    float Qc = Qs[p];
+    const uint32_t tag = (uint32_t)epoch;
+    for (int64_t e = e0; e < e1; ++e) {
+        const uint32_t i = (uint32_t)src[e];
+        const uint32_t j = (uint32_t)dst[e];
+        const uint32_t il = i - base;
+        Vec<D> yi = load_row<D>(Y, i);
+        int s = 0;
+        if (j != i) {
+            uint32_t o[3] = {j, 0u, 0u};
+            const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
+            if (k.nu >= 1) {
+                noise_pair(key0, key1, (uint64_t)e, tag, 0, il, Np, o[1], o[2]);
+                o[1] += base;
+                o[2] += base;
+            }
+            run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
+            s = cnt - 1;
+        } else {
+            const float ws = nce_weight(0.f, true, k, Qc);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const float dx = clip4(0.f * ws);
+                yi.v[c] = (yi.v[c] + dx) - dx;
+            }
+        }
+        for (; s < k.nu; s += 4) {
+            uint32_t o[4];
+            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), il, Np, o[0], o[1]);
+            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, il, Np, o[2], o[3]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) o[t] += base;
+            run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
+        }
+        store_row<D>(Y, i, yi);
+    }
+    chain_q[chain] = Qc;
+}
+
+// Qs[p] = mean of problem p's chain copies (FP64), one block per problem.
+__global__ void reduce_q_batched(const float *__restrict__ chain_q, const int64_t *__restrict__ cp,
+                                 float *__restrict__ Qs) {
+    __shared__ double red[32];
+    const int p = blockIdx.x;
+    double s = 0;
+    for (int64_t c = cp[p] + threadIdx.x; c < cp[p + 1]; c += blockDim.x) s += chain_q[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        Qs[p] = (float)(t / (double)(cp[p + 1] - cp[p]));
+    }
+}
+
 // Q = (sum of the chains' copies) / chains, as the reference's epoch-end
 // average over threads (src/ncvis.cpp:342-349).
 __global__ void reduce_q(const double *__restrict__ q_part, int blocks, int64_t chains,
@@ -425,6 +501,49 @@ void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const siz
         }
         NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, blocks, total_chains, g.Q);
     }
+}
+
+void run_sgd_hogwild_batched(const SgdBatch &g, const size_t *n_noise, cudaStream_t s) {
+    require(g.d >= 1 && g.d <= 4, "batched optimize: d must be in [1, 4]");
+    uint32_t key0, key1;
+    noise_key(g.seed, key0, key1);
+    const unsigned blocks = ceil_div(g.n_chains, kThreads);
+    for (int ep = 0; ep < g.n_epochs; ++ep) {
+        SgdArgs one{0, g.d, 0, nullptr, nullptr, nullptr, nullptr, g.seed, g.n_epochs,
+                    g.a, g.b, g.alpha, g.alpha_Q};
+        EpochConst k = epoch_const(one, ep, (int)n_noise[ep]);
+        switch (g.d) {
+            case 1:
+                NCVIS_LAUNCH(sgd_epoch_batched<1>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.off,
+                             g.eoff, g.cp, g.B, g.n_chains, g.Qs, g.chain_q, k, ep, key0, key1);
+                break;
+            case 2:
+                NCVIS_LAUNCH(sgd_epoch_batched<2>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.off,
+                             g.eoff, g.cp, g.B, g.n_chains, g.Qs, g.chain_q, k, ep, key0, key1);
+                break;
+            case 3:
+                NCVIS_LAUNCH(sgd_epoch_batched<3>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.off,
+                             g.eoff, g.cp, g.B, g.n_chains, g.Qs, g.chain_q, k, ep, key0, key1);
+                break;
+            default:
+                NCVIS_LAUNCH(sgd_epoch_batched<4>, blocks, kThreads, 0, s, g.Y, g.src, g.dst, g.off,
+                             g.eoff, g.cp, g.B, g.n_chains, g.Qs, g.chain_q, k, ep, key0, key1);
+        }
+        NCVIS_LAUNCH(reduce_q_batched, g.B, 256, 0, s, g.chain_q, g.cp, g.Qs);
+    }
+}
+
+int64_t sgd_batched_resident_chains(int d) {
+    int blocks = 0;
+    cudaError_t err;
+    switch (d) {
+        case 1: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch_batched<1>, kThreads, 0); break;
+        case 2: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch_batched<2>, kThreads, 0); break;
+        case 3: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch_batched<3>, kThreads, 0); break;
+        default: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sgd_epoch_batched<4>, kThreads, 0);
+    }
+    if (err != cudaSuccess || blocks < 1) blocks = 1;
+    return (int64_t)blocks * kThreads * num_sms();
 }
 
 void launch_sgd_replay(const SgdArgs &g, int epoch, size_t nu, int64_t edge_begin,

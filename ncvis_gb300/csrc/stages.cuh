@@ -19,6 +19,15 @@ enum Distance { kSquaredL2 = 0, kInnerProduct = 1, kCosine = 2, kCorrelation = 3
 void launch_preprocess(const float *X, int64_t N, int D, int dist, float *Xp, float *sqnorm,
                        __nv_bfloat16 *Xb, int ldb, int *bad_flag, cudaStream_t s);
 
+// Independent problems packed in one point array: problem p owns rows
+// [offsets[p], offsets[p+1]) (device arrays).  B == 0: one problem, all rows.
+struct Segments {
+    const int64_t *offsets = nullptr;      // [B+1]
+    const int64_t *tile_prefix = nullptr;  // [B+1] query tiles of the kNN kernel per problem
+    int B = 0;
+    int64_t n_tiles = 0;
+};
+
 // ---- K3 exact FP32 candidate selection + K4 rerank ---------------------------
 struct KnnPlan {
     int R;       // candidates kept per (point, split)
@@ -28,7 +37,9 @@ struct KnnPlan {
 KnnPlan plan_knn_f32(int64_t N, int k, int rerank_factor);
 // cand_i/cand_d: [N, plan.C()]; -1 marks an empty slot.
 void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int D, int dist,
-                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s);
+                           const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s,
+                           const Segments &seg = Segments());
+int knn_f32_query_tile();
 // Exact distances of the candidates, top k+1 by (distance, index), smallest
 // dropped, k written in descending order: inds/dists [N, k].
 void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,
@@ -68,6 +79,15 @@ void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t 
                         uint64_t seed, int n_init_epochs, float alpha, float *Y, void *workspace,
                         cudaStream_t s);
 
+// Batched problems (rows [off[p], off[p+1]), seeds[p]); tp[p] = first row tile
+// of problem p, tiles of init_tile_rows() rows never straddle problems.
+int init_tile_rows();
+size_t init_batched_workspace_bytes(int64_t total_rows, int64_t n_tiles, int B, int d);
+void run_init_embedding_batched(int64_t total_rows, int d, const int64_t *off, const int64_t *tp,
+                                int B, int64_t n_tiles, const uint64_t *seeds,
+                                const int64_t *row_ptr, const int32_t *cols, int n_init_epochs,
+                                float alpha, float *Y, void *workspace, cudaStream_t s);
+
 // ---- K7 SGD (src/ncvis.cpp:275-352) -------------------------------------------
 struct SgdArgs {
     int64_t N;
@@ -85,6 +105,22 @@ size_t sgd_workspace_bytes(int chains);
 int sgd_default_chains(int64_t E, int d);
 void run_sgd_hogwild(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s);
+// Batched Hogwild: problem p owns rows [off[p], off[p+1]), edges
+// [eoff[p], eoff[p+1]) and chains [cp[p], cp[p+1]) (device arrays); Qs[B] and
+// chain_q[n_chains] device floats.  d <= 4.
+struct SgdBatch {
+    int d;
+    int B;
+    int64_t n_chains;
+    const int32_t *src, *dst;
+    const int64_t *off, *eoff, *cp;
+    float *Y, *Qs, *chain_q;
+    uint64_t seed;
+    int n_epochs;
+    float a, b, alpha, alpha_Q;
+};
+void run_sgd_hogwild_batched(const SgdBatch &g, const size_t *n_noise, cudaStream_t s);
+int64_t sgd_batched_resident_chains(int d);
 // *err (device int) is set to 1 if an index outside [0, N) is met.
 void launch_sgd_replay(const SgdArgs &args, int epoch, size_t nu, int64_t edge_begin,
                        int64_t edge_end, const int32_t *stream, int64_t stream_offset, int *err,
