@@ -207,6 +207,22 @@ int ncvis_nce_grad_device(size_t N, size_t d, size_t E, const int32_t *d_src, co
 int ncvis_nce_noise_device(size_t N, size_t E, const int32_t *d_src, size_t n_noise, uint64_t seed,
                            uint32_t tag, uint64_t edge_offset, int32_t *d_out, void *stream);
 
+/* ncvis_nce_loss_device without any device allocation, for callers that
+ * cannot allocate device memory when they need the loss (a process whose
+ * memory pool already holds all free HBM, a latency-critical loop that must
+ * not take the allocator's synchronisation, a framework that forbids
+ * allocations outside its own pool).  Same arguments and result.  Its scratch
+ * is one fixed 64 KiB device array inside the library (kept on every GPU that
+ * loads it until exit), so E <= 2^20 per call; larger E is rejected.  The
+ * first call on each device looks up that array's device address; make it
+ * before any stream capture.  Calls share the array: calls whose GPU work
+ * overlaps in time race.  No counterpart in the reference (an addition).
+ * Errors: ncvis_get_last_error(). */
+int ncvis_nce_loss_device_noalloc(size_t N, size_t d, size_t E, const int32_t *d_src,
+                                  const int32_t *d_dst, const float *dY, const float *dQ,
+                                  size_t n_noise, float a, float b, uint64_t seed, uint32_t tag,
+                                  uint64_t edge_offset, double *d_loss, void *stream);
+
 /* Number of kernels this library has launched in the process so far. */
 uint64_t ncvis_kernel_launch_count(void);
 

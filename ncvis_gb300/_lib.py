@@ -118,6 +118,9 @@ SIGNATURES = {
                                         _vp, _vp]),
     "ncvis_nce_noise_device": (C.c_int, [_sz, _sz, _vp, _sz, C.c_uint64, C.c_uint32, C.c_uint64,
                                          _vp, _vp]),
+    "ncvis_nce_loss_device_noalloc": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, _sz,
+                                                C.c_float, C.c_float, C.c_uint64, C.c_uint32,
+                                                C.c_uint64, _vp, _vp]),
     "ncvis_kernel_launch_count": (C.c_uint64, []),
     "ncvis_version": (C.c_char_p, []),
 }
