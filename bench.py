@@ -42,10 +42,15 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--knn", choices=["fp32", "bf16"], default=os.environ.get("NCVIS_BENCH_KNN", "fp32"))
+    p.add_argument("--knn", choices=["fp32", "bf16"], default="bf16")
     p.add_argument("--n", type=int, default=N_FULL, help="points (default: the full workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-recall", action="store_true")
+    p.add_argument("--workload", choices=["fit", "nce", "batched"], default="fit",
+                   help="fit: the headline fit_transform; nce: the differentiable loss at "
+                        "N=200,000; batched: 256 independent embeddings in one run")
+    p.add_argument("--no-quality", action="store_true",
+                   help="skip the quality comparison against the plain FP32 path")
     return p.parse_args()
 
 
@@ -315,9 +320,34 @@ def run_ours(args):
     hbm = peaks.get("hbm_gbs", 6800.0)
 
     recall = None
+    inds = None
     if not args.no_recall:
         inds, _ = stages.knn(Xd, K_NN, 2, precision=1 if args.knn == "bf16" else 0)
         recall = recall_at_15(X, inds.cpu().numpy())
+
+    quality = None
+    if not args.no_quality:
+        # Embedding quality at k=15 of this path and of the plain FP32 path
+        # (one extra fit): kNN preservation on all points (exact kNN of X and
+        # of Y on the GPU) and trustworthiness on a 10,000-point sample.
+        from ncvis_gb300 import quality as Qm
+        Y_ours = vis.fit_transform(Xd)
+        plain = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
+                            random_seed=42, distance="cosine", knn_precision="fp32")
+        Y_plain = plain.fit_transform(Xd)
+        # X's table: the one measured above against FP64 (recall_at_15), else exact FP32.
+        x_inds = inds if inds is not None else stages.knn(Xd, K_NN, 2, precision=0)[0]
+        sub = np.sort(np.random.default_rng(1).choice(n, min(n, 10000), replace=False))
+        Xs = X[sub] / np.linalg.norm(X[sub], axis=1, keepdims=True)
+        quality = {
+            "k": K_NN,
+            "knn_preservation_full": {
+                "this_path": Qm.knn_preservation_device(Xd, Y_ours, K_NN, 2, x_inds=x_inds),
+                "plain_fp32_path": Qm.knn_preservation_device(Xd, Y_plain, K_NN, 2, x_inds=x_inds)},
+            "trustworthiness_sample10k": {
+                "this_path": Qm.trustworthiness(Xs, Y_ours[sub].cpu().numpy(), K_NN),
+                "plain_fp32_path": Qm.trustworthiness(Xs, Y_plain[sub].cpu().numpy(), K_NN)},
+        }
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -338,6 +368,7 @@ def run_ours(args):
                 "algorithmic_GBps": sgd_gbs, "hbm_peak_GBps": hbm, "frac_of_hbm": sgd_gbs / hbm,
                 "E": E},
         "recall_at_15": recall,
+        "quality": quality,
         "stage_ms": {k: statistics.mean(s[k] for s in stage_list) for k in
                      ("preprocess_ms", "knn_ms", "rerank_ms", "symmetrize_ms", "init_ms",
                       "optimize_ms")},
@@ -352,10 +383,107 @@ def run_ours(args):
     return 0
 
 
+def run_nce(args):
+    """Forward + backward of the NCE loss (torch.autograd.Function over the
+    engine's kernels) over the symmetrized 15-NN graph of a 200,000-point,
+    64-D, 10-component Gaussian mixture, Y ~ N(0, 1e-4 I), Q = 1, 5 noise
+    samples per edge, batches of 2^20 edges; one step = one pass over all
+    edges.  Throughput in (positive + noise) samples per second."""
+    import torch
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300 import nce, stages
+    from ncvis_gb300.synthetic import gaussian_mixture
+    dev = torch.device("cuda", 0)
+    X, _ = gaussian_mixture(200_000, 64, 10, 5.0, 1.0, seed=42)
+    inds, dists = stages.knn(torch.from_numpy(X).to(dev), 15, 0)
+    _, cols, _, src = stages.symmetrize(inds, dists)
+    E = src.shape[0]
+    batch = 1 << 20
+    lines = []
+    for d in (2, 16):
+        g = torch.Generator(device=dev).manual_seed(0)
+        Y = (1e-2 * torch.randn((200_000, d), device=dev, generator=g)).requires_grad_(True)
+        Q = torch.tensor(1.0, device=dev, requires_grad=True)
+
+        def step(it):
+            for b0 in range(0, E, batch):
+                loss = nce.nce_loss(Y, Q, src[b0:b0 + batch], cols[b0:b0 + batch], n_noise=5,
+                                    seed=it, edge_offset=b0)
+                loss.backward()
+        for it in range(args.warmup):
+            step(it)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for it in range(args.steps):
+            step(100 + it)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        samples = E * 6
+        lines.append({"d": d, "ms_per_pass": ms, "samples_per_s": samples / (ms / 1e3),
+                      "edges": int(E), "batches": (E + batch - 1) // batch})
+    print(json.dumps({"metric": "nce_fwd_bwd_samples_per_s", "value": lines[0]["samples_per_s"],
+                      "unit": "samples/s", "higher_is_better": True, "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
+                      "data": "synthetic (seeded Gaussian mixture)",
+                      "config": {"workload": "NCE loss fwd+bwd, N=200000 D=64 GMM 15-NN graph, "
+                                             "5 noise samples, batches of 2^20 edges"},
+                      "per_dim": lines}), flush=True)
+    return 0
+
+
+def run_batched(args):
+    """256 independent embeddings (N log-uniform in [500, 50000], D=64
+    Gaussian mixtures with 4-20 components, per-problem seeds, k=15, d=2,
+    50 epochs) in one run, against looping the single-problem path; pair
+    updates per second over the whole job."""
+    import torch
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300.synthetic import gaussian_mixture
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(42)
+    sizes = np.exp(rng.uniform(np.log(500), np.log(50000), 256)).astype(int)
+    Xs = [torch.from_numpy(gaussian_mixture(int(n), 64, int(rng.integers(4, 21)), 5.0, 1.0,
+                                            seed=42 + p)[0]).to(dev) for p, n in enumerate(sizes)]
+    seeds = list(range(42, 42 + len(Xs)))
+    vis = ncvis.NCVis(random_seed=42)
+    for _ in range(args.warmup):
+        vis.fit_transform_batched(Xs, seeds=seeds)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vis.fit_transform_batched(Xs, seeds=seeds)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    st = vis.stage_times()
+    plan_sum = int((vis.noise_plan.astype(np.int64) + 1).sum())
+    updates = st["n_edges"] * plan_sum
+    t0 = time.perf_counter()
+    for p, x in enumerate(Xs):
+        ncvis.NCVis(random_seed=42 + p).fit_transform(x)
+    torch.cuda.synchronize()
+    loop = time.perf_counter() - t0
+    print(json.dumps({"metric": "batched_pair_updates_per_s", "value": updates / wall,
+                      "unit": "pair-updates/s", "higher_is_better": True, "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
+                      "data": "synthetic (seeded Gaussian mixtures)",
+                      "config": {"workload": "256 embeddings, N log-uniform [500, 50000], D=64, "
+                                             "k=15, d=2, 50 epochs", "total_N": int(sizes.sum())},
+                      "wall_s": wall, "stage_ms": st, "loop_of_single_fits_s": loop,
+                      "loop_pair_updates_per_s": updates / loop, "speedup_vs_loop": loop / wall}),
+          flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "nce":
+        return run_nce(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

@@ -79,7 +79,7 @@ typedef struct ncvis_params {
  * FP32 exact kNN, Hogwild SGD, engine-owned stream, automatic chain count). */
 typedef struct ncvis_options {
     int knn_precision;      /* NCVIS_KNN_FP32 | NCVIS_KNN_BF16_RERANK */
-    int rerank_factor;      /* candidates kept per point = rerank_factor * k (0: 2 for FP32, 4 for BF16) */
+    int rerank_factor;      /* candidates kept per point ~ rerank_factor * k (0: 2; BF16 keeps 32 or 64) */
     int sgd_mode;           /* NCVIS_SGD_HOGWILD | NCVIS_SGD_REPLAY */
     const int32_t *replay_stream; /* host array of noise indices in one-thread draw order (replay) */
     size_t replay_len;      /* entries in replay_stream: E * sum(n_noise) */

@@ -147,10 +147,18 @@ def lib():
     return _lib
 
 
-def check(rc: int, handle=None) -> None:
-    """Raise NcvisError for a non-zero status."""
+def error_of(rc: int, handle=None):
+    """The NcvisError for a non-zero status (None for NCVIS_OK), with the
+    message the library recorded for it."""
     if rc == NCVIS_OK:
-        return
+        return None
     L = lib()
     msg = L.ncvis_last_error(handle) if handle else L.ncvis_get_last_error()
-    raise NcvisError(rc, (msg or b"").decode(errors="replace") or f"ncvis status {rc}")
+    return NcvisError(rc, (msg or b"").decode(errors="replace") or f"ncvis status {rc}")
+
+
+def check(rc: int, handle=None) -> None:
+    """Raise NcvisError for a non-zero status."""
+    err = error_of(rc, handle)
+    if err:
+        raise err

@@ -158,8 +158,10 @@ class NCVis:
                 rc = L.ncvis_fit_transform_device(self._h, Xc.data_ptr(), Xc.shape[0],
                                                   Xc.shape[1] if Xc.dim() > 1 else 0,
                                                   Y.data_ptr())
+                err = _lib.error_of(rc, self._h)
                 self._set_stream(None)
-            _lib.check(rc, self._h)
+            if err:
+                raise err
             return Y
         Xn = np.ascontiguousarray(X, dtype=np.float32)
         if Xn.ndim != 2:
@@ -169,6 +171,50 @@ class NCVis:
                                    Y.ctypes.data)
         _lib.check(rc, self._h)
         return Y
+
+    def fit_transform_batched(self, Xs, seeds=None):
+        """Embeds several independent datasets in one run (each as if it were
+        embedded alone, with its own seed) and returns one Y per dataset.
+        numpy inputs give numpy outputs; CUDA tensors give CUDA tensors.  The
+        neighbour count is clamped by the smallest dataset; FP32 kNN, d <= 4."""
+        import torch
+        L = _lib.lib()
+        cuda_in = all(_is_cuda_tensor(x) for x in Xs)
+        if cuda_in:
+            dev = Xs[0].device
+            parts = [x.detach().to(torch.float32).contiguous() for x in Xs]
+        else:
+            dev = torch.device("cuda", torch.cuda.current_device())
+            parts = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)) for x in Xs]
+        if not parts or any(p.dim() != 2 for p in parts):
+            raise ValueError("Xs must be a non-empty list of 2-D arrays")
+        D = parts[0].shape[1]
+        if any(p.shape[1] != D for p in parts):
+            raise ValueError("all datasets must have the same number of features")
+        sizes = [p.shape[0] for p in parts]
+        offsets = np.zeros(len(parts) + 1, dtype=np.int64)
+        offsets[1:] = np.cumsum(sizes)
+        X = torch.cat(parts).to(dev)
+        Y = torch.empty((int(offsets[-1]), self.d), dtype=torch.float32, device=dev)
+        seed_arr = None
+        if seeds is not None:
+            seed_arr = np.ascontiguousarray(seeds, dtype=np.uint64)
+            if seed_arr.shape != (len(parts),):
+                raise ValueError("one seed per dataset")
+        with torch.cuda.device(dev):
+            self._set_stream(torch.cuda.current_stream().cuda_stream)
+            rc = L.ncvis_fit_transform_batched_device(
+                self._h, X.data_ptr(), D, offsets.ctypes.data, len(parts),
+                seed_arr.ctypes.data if seed_arr is not None else None, Y.data_ptr())
+            err = _lib.error_of(rc, self._h)
+            self._set_stream(None)
+        if err:
+            raise err
+        out = torch.split(Y, sizes)
+        if cuda_in:
+            return list(out)
+        torch.cuda.current_stream(dev).synchronize()
+        return [y.cpu().numpy() for y in out]
 
     def stage_times(self) -> dict:
         """Device times (ms) of the stages of the last fit_transform."""

@@ -505,7 +505,9 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         for (size_t q = 0; q < B; ++q) {
             const int64_t Ep = h_eoff[q + 1] - h_eoff[q];
             int64_t c = (int64_t)((double)target * (double)Ep / (double)std::max<int64_t>(E, 1));
+            const int64_t Np = h_off[q + 1] - h_off[q];
             c = std::max<int64_t>(1, std::min<int64_t>(c, std::max<int64_t>(Ep / 16, 1)));
+            c = std::min<int64_t>(c, std::max<int64_t>(Np / 8, 1));
             cp[q + 1] = cp[q] + c;
         }
         return cp[B];
@@ -787,6 +789,8 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
         require(d_src && d_dst && dY && dQ && n_noise, "optimize: null pointer");
         require(N >= 2 && d >= 1 && d <= 32, "optimize: need N >= 2 and 1 <= d <= 32");
         require(((uintptr_t)dY & 7) == 0, "optimize: Y must be 8-byte aligned");
+        require((((uintptr_t)d_src | (uintptr_t)d_dst) & 15) == 0,
+                "optimize: src and dst must be 16-byte aligned");
         require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
                 "optimize: need 0 <= epoch_begin <= epoch_end <= n_epochs");
         cudaStream_t s = (cudaStream_t)stream;
@@ -794,7 +798,7 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
         require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
                     indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
                 "optimize: an edge endpoint is outside [0, N)");
-        if (chains <= 0) chains = sgd_default_chains((int64_t)E, (int)d);
+        if (chains <= 0) chains = sgd_default_chains((int64_t)E, (int64_t)N, (int)d);
         void *ws = nullptr;
         NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
         SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,

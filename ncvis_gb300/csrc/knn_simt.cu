@@ -11,11 +11,12 @@
 // problems use one candidate range; small ones split the range so that the
 // grid fills the GPU, and K4 merges the splits.
 //
-// K4 (rerank): one warp per point recomputes the exact distance of each
-// candidate the way the hnswlib spaces do (sum of squared differences, or
-// 1 - dot, accumulated left to right in FP32), ranks the candidates by
-// (distance, index), drops rank 0 and writes ranks k..1, i.e. the k farthest
-// of the k+1 nearest in descending order, as findKNN stores them.
+// K4 (rerank): one warp per point recomputes the exact FP32 distance of each
+// candidate the way the hnswlib spaces define it (sum of squared
+// differences, or 1 - dot; coordinates summed per lane, then across the
+// warp), ranks the candidates by (distance, index), drops rank 0 and writes
+// ranks k..1, i.e. the k farthest of the k+1 nearest in descending order, as
+// findKNN stores them.
 #include <algorithm>
 #include <cfloat>
 
@@ -213,8 +214,11 @@ __global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ X
     }
 }
 
-// One warp per point.  Candidate distances are recomputed exactly, then
-// ranked; C <= 1024.
+// One warp per point.  The query row is spread over the lanes (coordinate
+// t in lane t % 32); each candidate row is read coalesced and its exact FP32
+// distance reduced across the warp (the same lane split for (i, j) and
+// (j, i), so d(i, j) == d(j, i)).  Candidates are then ranked; C <= 1024.
+template <int T>  // ceil(D / 32) coordinates per lane, T <= 4; T == 0: any D
 __global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp, int64_t N, int D,
                                                    int dist, const int32_t *__restrict__ cand_i,
                                                    int C, int k, int32_t *__restrict__ inds,
@@ -226,25 +230,70 @@ __global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp,
     int *si = (int *)(sd + C);
     if (row >= N) return;
     const float *q = Xp + row * D;
-    for (int c = lane; c < C; c += 32) {
-        const int idx = cand_i[row * C + c];
-        float dv = FLT_MAX;
-        if (idx >= 0) {
-            const float *y = Xp + (int64_t)idx * D;
-            float acc = 0.f;
-            if (dist == kSquaredL2) {
-                for (int t = 0; t < D; ++t) {
-                    const float diff = __fsub_rn(q[t], y[t]);
-                    acc = __fadd_rn(acc, __fmul_rn(diff, diff));
+    const bool l2 = (dist == kSquaredL2);
+    float qv[T > 0 ? T : 1];
+    if (T > 0) {
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const int c = lane + 32 * t;
+            qv[t] = c < D ? q[c] : 0.f;
+        }
+    }
+    constexpr int U = 4;  // candidates in flight per warp
+    for (int c0 = 0; c0 < C; c0 += U) {
+        int idx[U];
+        float part[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            idx[u] = (c0 + u < C) ? cand_i[row * C + c0 + u] : -1;  // warp-uniform
+            part[u] = 0.f;
+        }
+        if (T > 0) {
+#pragma unroll
+            for (int t = 0; t < T; ++t) {
+                const int col = lane + 32 * t;
+                float yv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    yv[u] = (idx[u] >= 0 && col < D) ? Xp[(int64_t)idx[u] * D + col] : 0.f;
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (col < D) {
+                        if (l2) {
+                            const float diff = __fsub_rn(qv[t], yv[u]);
+                            part[u] = __fadd_rn(part[u], __fmul_rn(diff, diff));
+                        } else {
+                            part[u] = __fadd_rn(part[u], __fmul_rn(qv[t], yv[u]));
+                        }
+                    }
                 }
-                dv = acc;
-            } else {
-                for (int t = 0; t < D; ++t) acc = __fadd_rn(acc, __fmul_rn(q[t], y[t]));
-                dv = __fsub_rn(1.f, acc);
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (idx[u] < 0) continue;
+                const float *y = Xp + (int64_t)idx[u] * D;
+                for (int col = lane; col < D; col += 32) {
+                    const float yv = y[col];
+                    if (l2) {
+                        const float diff = __fsub_rn(q[col], yv);
+                        part[u] = __fadd_rn(part[u], __fmul_rn(diff, diff));
+                    } else {
+                        part[u] = __fadd_rn(part[u], __fmul_rn(q[col], yv));
+                    }
+                }
             }
         }
-        sd[c] = dv;
-        si[c] = idx;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                part[u] = __fadd_rn(part[u], __shfl_xor_sync(0xffffffffu, part[u], o));
+            if (lane == 0 && c0 + u < C) {
+                sd[c0 + u] = idx[u] >= 0 ? (l2 ? part[u] : __fsub_rn(1.f, part[u])) : FLT_MAX;
+                si[c0 + u] = idx[u];
+            }
+        }
     }
     __syncwarp();
     for (int c = lane; c < C; c += 32) {
@@ -307,12 +356,21 @@ void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *c
     const size_t smem = (size_t)warps * C * 8;
     static size_t configured = 0;
     if (smem > configured) {
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    NCVIS_LAUNCH(rerank_rows, ceil_div(N, warps), warps * 32, smem, s, Xp, N, D, dist, cand_i, C,
-                 k, inds, dists);
+    const unsigned grid = ceil_div(N, warps);
+    switch ((D + 31) / 32) {
+        case 1: NCVIS_LAUNCH(rerank_rows<1>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
+        case 2: NCVIS_LAUNCH(rerank_rows<2>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
+        case 3: NCVIS_LAUNCH(rerank_rows<3>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
+        case 4: NCVIS_LAUNCH(rerank_rows<4>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
+        default: NCVIS_LAUNCH(rerank_rows<0>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists);
+    }
 }
 
 }  // namespace ncvis_gpu

@@ -138,6 +138,96 @@ __device__ __forceinline__ void run_group(float *Y, Vec<D> &yi, const uint32_t (
     }
 }
 
+// One edge of a chain: the positive sample and its noise samples, with y_i
+// held in registers by the caller.
+template <int D>
+__device__ __forceinline__ void run_edge(float *Y, Vec<D> &yi, uint32_t i, uint32_t j, int64_t e,
+                                         uint32_t N, uint32_t lo, const EpochConst &k, float &Qc,
+                                         uint32_t key0, uint32_t key1, uint32_t tag) {
+    int s = 0;  // next noise sample
+    if (j != i) {
+        // The positive sample and the first noise pair share one group.
+        uint32_t o[3] = {j, 0u, 0u};
+        const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
+        if (k.nu >= 1) {
+            noise_pair(key0, key1, (uint64_t)e, tag, 0, i - lo, N, o[1], o[2]);
+            o[1] += lo;
+            o[2] += lo;
+        }
+        run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
+        s = cnt - 1;
+    } else {
+        // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
+        const float ws = nce_weight(0.f, true, k, Qc);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const float dx = clip4(0.f * ws);
+            yi.v[c] = (yi.v[c] + dx) - dx;
+        }
+    }
+    // Remaining noise samples in groups of four (two Philox blocks each).
+    for (; s < k.nu; s += 4) {
+        uint32_t o[4];
+        noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), i - lo, N, o[0], o[1]);
+        noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, i - lo, N, o[2], o[3]);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) o[t] += lo;
+        run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
+    }
+}
+
+// A chain's edges [e0, e1) (e0 a multiple of 4): edge indices come in aligned
+// groups of four, the next group loaded while the current one runs; y_i stays
+// in registers while consecutive edges share their source row and is written
+// back when the row changes (other chains' updates of that row in between are
+// lost, as lock-free updates may be).
+template <int D>
+__device__ __forceinline__ void run_chain(float *Y, const int32_t *__restrict__ src,
+                                          const int32_t *__restrict__ dst, int64_t e0, int64_t e1,
+                                          uint32_t N, uint32_t lo, const EpochConst &k, float &Qc,
+                                          uint32_t key0, uint32_t key1, uint32_t tag) {
+    if (e0 >= e1) return;
+    auto load4 = [&](int64_t e, int4 &s4, int4 &d4) {
+        if (e + 4 <= e1) {
+            s4 = __ldg(reinterpret_cast<const int4 *>(src + e));
+            d4 = __ldg(reinterpret_cast<const int4 *>(dst + e));
+        } else {
+            s4.x = src[e];
+            d4.x = dst[e];
+            s4.y = e + 1 < e1 ? src[e + 1] : 0;
+            d4.y = e + 1 < e1 ? dst[e + 1] : 0;
+            s4.z = e + 2 < e1 ? src[e + 2] : 0;
+            d4.z = e + 2 < e1 ? dst[e + 2] : 0;
+            s4.w = e + 3 < e1 ? src[e + 3] : 0;
+            d4.w = e + 3 < e1 ? dst[e + 3] : 0;
+        }
+    };
+    int4 s4, d4;
+    load4(e0, s4, d4);
+    uint32_t cur = (uint32_t)s4.x;
+    Vec<D> yi = load_row<D>(Y, cur);
+    for (int64_t e = e0; e < e1; e += 4) {
+        int4 ns4 = s4, nd4 = d4;
+        if (e + 4 < e1) load4(e + 4, ns4, nd4);
+        const int32_t sv[4] = {s4.x, s4.y, s4.z, s4.w};
+        const int32_t dv[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (e + q >= e1) break;
+            const uint32_t i = (uint32_t)sv[q];
+            if (i != cur) {
+                store_row<D>(Y, cur, yi);
+                cur = i;
+                yi = load_row<D>(Y, cur);
+            }
+            run_edge<D>(Y, yi, i, (uint32_t)dv[q], e + q, N, lo, k, Qc, key0, key1, tag);
+        }
+        s4 = ns4;
+        d4 = nd4;
+    }
+    store_row<D>(Y, cur, yi);
+}
+
 template <int D>
 __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                                                       const int32_t *__restrict__ src,
@@ -147,40 +237,10 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch(float *__restrict__ Y,
                                                       int epoch, uint32_t key0, uint32_t key1,
                                                       int64_t chunk, int64_t n_chains) {
     const int64_t chain = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-    const int64_t e0 = chain < n_chains ? chain * chunk : E;
+    const int64_t e0 = chain < n_chains ? min(E, chain * chunk) : E;
     const int64_t e1 = min(E, e0 + chunk);
     float Qc = *Q_in;
-    const uint32_t tag = (uint32_t)epoch;
-    for (int64_t e = e0; e < e1; ++e) {
-        const uint32_t i = (uint32_t)src[e];
-        const uint32_t j = (uint32_t)dst[e];
-        Vec<D> yi = load_row<D>(Y, i);
-        int s = 0;  // next noise sample
-        if (j != i) {
-            // The positive sample and the first noise pair share one group.
-            uint32_t o[3] = {j, 0u, 0u};
-            const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
-            if (k.nu >= 1) noise_pair(key0, key1, (uint64_t)e, tag, 0, i, N, o[1], o[2]);
-            run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
-            s = cnt - 1;
-        } else {
-            // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
-            const float ws = nce_weight(0.f, true, k, Qc);
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const float dx = clip4(0.f * ws);
-                yi.v[c] = (yi.v[c] + dx) - dx;
-            }
-        }
-        // Remaining noise samples in groups of four (two Philox blocks each).
-        for (; s < k.nu; s += 4) {
-            uint32_t o[4];
-            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), i, N, o[0], o[1]);
-            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, i, N, o[2], o[3]);
-            run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
-        }
-        store_row<D>(Y, i, yi);
-    }
+    run_chain<D>(Y, src, dst, e0, e1, N, 0u, k, Qc, key0, key1, (uint32_t)epoch);
     // Chain copies of Q, summed in FP64 per block.
     __shared__ double red[kThreads / 32];
     double v = chain < n_chains ? (double)Qc : 0.0;
@@ -251,46 +311,24 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch_batched(
     const int p = segment_of(cp, B, chain);
     const int64_t lc = chain - cp[p], nc = cp[p + 1] - cp[p];
     const int64_t Ep = eoff[p + 1] - eoff[p];
-    const int64_t chunk = (Ep + nc - 1) / nc;
-    const int64_t e0 = eoff[p] + min(Ep, lc * chunk);
-    const int64_t e1 = eoff[p] + min(Ep, (lc + 1) * chunk);
-    const uint32_t base = (uint32_t)off[p];
+    const int64_t chunk = ((Ep + nc - 1) / nc + 3) & ~(int64_t)3;
+    // Aligned to 4 relative to the global edge array: shift by the problem's misalignment.
+    const int64_t base = eoff[p];
+    int64_t e0 = base + min(Ep, lc * chunk);
+    int64_t e1 = base + min(Ep, (lc + 1) * chunk);
+    const uint32_t lo = (uint32_t)off[p];
     const uint32_t Np = (uint32_t)(off[p + 1] - off[p]);
     float Qc = Qs[p];
-    const uint32_t tag = (uint32_t)epoch;
-    for (int64_t e = e0; e < e1; ++e) {
-        const uint32_t i = (uint32_t)src[e];
-        const uint32_t j = (uint32_t)dst[e];
-        const uint32_t il = i - base;
-        Vec<D> yi = load_row<D>(Y, i);
-        int s = 0;
-        if (j != i) {
-            uint32_t o[3] = {j, 0u, 0u};
-            const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
-            if (k.nu >= 1) {
-                noise_pair(key0, key1, (uint64_t)e, tag, 0, il, Np, o[1], o[2]);
-                o[1] += base;
-                o[2] += base;
-            }
-            run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
-            s = cnt - 1;
-        } else {
-            const float ws = nce_weight(0.f, true, k, Qc);
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const float dx = clip4(0.f * ws);
-                yi.v[c] = (yi.v[c] + dx) - dx;
-            }
+    if (e0 < e1) {
+        // Leading edges up to the next multiple of 4 run one by one.
+        const int64_t a = min(e1, (e0 + 3) & ~(int64_t)3);
+        for (int64_t e = e0; e < a; ++e) {
+            Vec<D> yi = load_row<D>(Y, (uint32_t)src[e]);
+            run_edge<D>(Y, yi, (uint32_t)src[e], (uint32_t)dst[e], e, Np, lo, k, Qc, key0, key1,
+                        (uint32_t)epoch);
+            store_row<D>(Y, (uint32_t)src[e], yi);
         }
-        for (; s < k.nu; s += 4) {
-            uint32_t o[4];
-            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), il, Np, o[0], o[1]);
-            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, il, Np, o[2], o[3]);
-#pragma unroll
-            for (int t = 0; t < 4; ++t) o[t] += base;
-            run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
-        }
-        store_row<D>(Y, i, yi);
+        run_chain<D>(Y, src, dst, a, e1, Np, lo, k, Qc, key0, key1, (uint32_t)epoch);
     }
     chain_q[chain] = Qc;
 }
@@ -453,10 +491,14 @@ int64_t resident_chains(int d) {
 
 }  // namespace
 
-int sgd_default_chains(int64_t E, int d) {
+int sgd_default_chains(int64_t E, int64_t N, int d) {
     // Every chain resident at once, each with at least ~64 edges so that its
-    // copy of Q follows many samples before the epoch average.
+    // copy of Q follows many samples before the epoch average, and at most one
+    // chain per 8 points: with more concurrent writers per point the lock-free
+    // updates start to overwrite each other and the embedding drifts from the
+    // reference's (measured on 300- and 10,000-point graphs).
     int64_t chains = std::min<int64_t>(resident_chains(d), std::max<int64_t>(E / 64, 1));
+    chains = std::min<int64_t>(chains, std::max<int64_t>(N / 8, 1));
     return (int)std::max<int64_t>(chains, 1);
 }
 
@@ -468,10 +510,10 @@ size_t sgd_workspace_bytes(int chains) {
 void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s) {
     require(g.N >= 2 && g.N < (int64_t(1) << 31), "optimize: N must be in [2, 2^31)");
-    if (chains <= 0) chains = sgd_default_chains(g.E, g.d);
+    if (chains <= 0) chains = sgd_default_chains(g.E, g.N, g.d);
     const int blocks = (int)ceil_div(chains, kThreads);
     const int64_t total_chains = chains;
-    const int64_t chunk = (g.E + total_chains - 1) / total_chains;
+    const int64_t chunk = ((g.E + total_chains - 1) / total_chains + 3) & ~(int64_t)3;
     double *q_part = (double *)workspace;
     uint32_t key0, key1;
     noise_key(g.seed, key0, key1);

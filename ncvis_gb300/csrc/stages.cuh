@@ -102,7 +102,7 @@ struct SgdArgs {
     float a, b, alpha, alpha_Q;
 };
 size_t sgd_workspace_bytes(int chains);
-int sgd_default_chains(int64_t E, int d);
+int sgd_default_chains(int64_t E, int64_t N, int d);
 void run_sgd_hogwild(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s);
 // Batched Hogwild: problem p owns rows [off[p], off[p+1]), edges

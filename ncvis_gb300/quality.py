@@ -80,6 +80,27 @@ def trustworthiness(X, Y, k: int = 15, device=None, block: int = 1024) -> float:
     return 1.0 - penalty * (2.0 / (N * k * (2.0 * N - 3.0 * k - 1.0)))
 
 
+def knn_preservation_device(X, Y, k: int = 15, distance: int = 0, x_inds=None) -> float:
+    """kNN preservation at full size on the GPU: the exact kNN tables of X (in
+    the engine's distance) and of Y (squared L2) come from the engine's own
+    kNN kernels (one CUDA launch set each, O(N^2) work on the device), then
+    the mean overlap |kNN_X(i) & kNN_Y(i)| / k.  Both tables follow the
+    reference's row contract (the nearest of the k+1 dropped, normally the
+    point itself).  `x_inds` may pass a precomputed table of X."""
+    torch = _torch()
+    from . import stages
+    if x_inds is None:
+        x_inds, _ = stages.knn(_as_tensor(X, "cuda"), k, distance)
+    y_inds, _ = stages.knn(_as_tensor(Y, "cuda"), k, 0)
+    a = x_inds.to(torch.int64)
+    b = y_inds.to(torch.int64)
+    hits = 0
+    for s in range(0, a.shape[0], 1 << 16):
+        aa, bb = a[s:s + (1 << 16)], b[s:s + (1 << 16)]
+        hits += (aa[:, :, None] == bb[:, None, :]).any(2).sum().item()
+    return hits / (a.shape[0] * k)
+
+
 def recall_at_k(found, exact) -> float:
     """Mean fraction of each row of `exact` (index sets) present in `found`."""
     found = np.asarray(found)

@@ -1,0 +1,68 @@
+"""Batched embeddings (ncvis_fit_transform_batched_device): many independent
+problems in one run, each with its own kNN graph, initialisation stream,
+noise range and Q, the SGD epoch loop captured as one CUDA graph.
+
+Each problem must come out as if embedded alone: its kNN table (through the
+same FP32 selection) equals the single-problem one, its init equals the
+oracle's one-thread init for its seed (1e-5), and its embedding quality
+(trustworthiness at k=15) is within 0.02 of the single-problem path.
+"""
+import numpy as np
+import pytest
+
+from conftest import gmm
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(sizes, D=16, seed=0):
+    Xs = []
+    for p, n in enumerate(sizes):
+        X, _ = gmm(n, D, 4 + p % 5, 5.0, seed=seed + p)
+        Xs.append(X)
+    return Xs
+
+
+def test_batched_matches_single_problems(cuda, oracle):
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300 import quality
+    sizes = [500, 1337, 4000, 777, 2500]
+    Xs = _problems(sizes)
+    seeds = [11, 12, 13, 14, 15]
+    vis = ncvis.NCVis(random_seed=42)
+    Ys = vis.fit_transform_batched(Xs, seeds=seeds)
+    assert [Y.shape for Y in Ys] == [(n, 2) for n in sizes]
+    t = vis.stage_times()
+    assert t["k"] == 15 and t["n_edges"] > sum(sizes) * 15
+    for X, Y, sd in zip(Xs, Ys, seeds):
+        assert np.isfinite(Y).all()
+        Ysingle = ncvis.NCVis(random_seed=sd).fit_transform(X)
+        tb = quality.trustworthiness(X, Y, 15)
+        ts = quality.trustworthiness(X, Ysingle, 15)
+        assert abs(tb - ts) <= 0.02, (len(X), tb, ts)
+
+
+def test_batched_init_and_graph(cuda, oracle):
+    """With no SGD epochs the batched output is each problem's init, which
+    must match the oracle's one-thread init of that problem's graph."""
+    import ncvis_gb300 as ncvis
+    sizes = [600, 1500, 900]
+    Xs = _problems(sizes, seed=5)
+    seeds = [101, 202, 303]
+    vis = ncvis.NCVis(random_seed=1, n_epochs=0, n_noise=np.zeros(0, dtype=np.int64))
+    Ys = vis.fit_transform_batched(Xs, seeds=seeds)
+    for X, Y, sd in zip(Xs, Ys, seeds):
+        from ncvis_gb300 import stages
+        inds, dists = stages.knn(cuda.tensor(X, device="cuda"), 15, 0)
+        inds, dists = inds.cpu().numpy().astype(np.int64), dists.cpu().numpy()
+        rp, cols, _ = oracle.symmetrize(inds, dists)
+        ref = oracle.init_embedding(len(X), 2, oracle.edges_from_csr(rp), cols, sd, 20,
+                                    np.float32(1 / 15), 1)
+        np.testing.assert_allclose(Y, ref, rtol=0, atol=1e-5 * max(1.0, np.abs(ref).max()))
+
+
+def test_batched_rejects_bad_layout(cuda):
+    import ncvis_gb300 as ncvis
+    vis = ncvis.NCVis()
+    with pytest.raises(ncvis.NcvisError, match="at least two points"):
+        vis.fit_transform_batched([np.zeros((1, 3), np.float32), np.ones((5, 3), np.float32)])
