@@ -37,14 +37,14 @@ namespace {
 
 constexpr int kQueryTile = 256;   // queries per CTA tile (2 x M=128)
 constexpr int kCandTile = 128;    // candidates per tile (N=128)
-constexpr int kStages = 4;        // candidate-tile ring
+constexpr int kStages = 3;        // candidate-tile ring
 constexpr int kAtomBytes = 128 * 128;  // 128 rows x 128 bytes (64 bf16) per swizzle atom column
 constexpr int kMaxAtoms = 2;      // K <= 128
 constexpr int kThreads = 320;
 constexpr int kEpiWarp0 = 2;
 constexpr int kEpiWarps = 8;
 constexpr int kEpiThreads = kEpiWarps * 32;
-constexpr int kChunk = 16;  // accumulator columns read per tcgen05.ld
+constexpr int kQueue = 32;  // per-row insertion queue slots (shared memory)
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -52,8 +52,8 @@ struct SharedStorage {
     // 1024-byte aligned tiles first (128B swizzle atoms repeat every 1024 B).
     uint8_t a[2][kMaxAtoms][kAtomBytes];
     uint8_t b[kStages][kMaxAtoms][kAtomBytes];
-    float stage_v[16][kEpiThreads];    // a chunk's qualifying scores, [slot][thread]
-    int32_t stage_i[16][kEpiThreads];  // and their candidate indices
+    float queue_v[kQueue][kEpiThreads];    // queued candidate scores, [slot][thread]
+    int32_t queue_i[kQueue][kEpiThreads];  // and their candidate indices
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t a_full, a_empty;
@@ -153,7 +153,7 @@ __device__ __forceinline__ void tmem_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[32]) {
     uint32_t r[32];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -165,11 +165,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
           "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -178,12 +179,44 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
           "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void tmem_wait_ld() {
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Minimum (kMax false) or maximum of n values, as a tree of 3-input operations.
+template <bool kMax, int n>
+__device__ __forceinline__ float tree_reduce(const float (&a)[n]) {
+    if constexpr (n == 1) {
+        return a[0];
+    } else if constexpr (n == 2) {
+        return kMax ? fmaxf(a[0], a[1]) : fminf(a[0], a[1]);
+    } else {
+        constexpr int m = (n + 2) / 3;
+        float b[m];
+#pragma unroll
+        for (int j = 0; j < m; ++j) {
+            if (3 * j + 2 < n)
+                b[j] = kMax ? max3f(a[3 * j], a[3 * j + 1], a[3 * j + 2])
+                            : min3f(a[3 * j], a[3 * j + 1], a[3 * j + 2]);
+            else if (3 * j + 1 < n)
+                b[j] = kMax ? fmaxf(a[3 * j], a[3 * j + 1]) : fminf(a[3 * j], a[3 * j + 1]);
+            else
+                b[j] = a[3 * j];
+        }
+        return tree_reduce<kMax, m>(b);
+    }
 }
 
 // Insert (v, vi) into the ascending list (ls, li) of R entries, dropping the
@@ -204,10 +237,31 @@ __device__ __forceinline__ void list_push(float (&ls)[R], int32_t (&li)[R], floa
     }
 }
 
+// Every queued candidate of the warp's rows goes into its row's list, in
+// lockstep rounds (one per slot of the fullest queue); queues end empty.
 template <int R>
+__device__ __forceinline__ void flush_queue(float (&ls)[R], int32_t (&li)[R], float &worst,
+                                            int &qlen, const float (*queue_v)[kEpiThreads],
+                                            const int32_t (*queue_i)[kEpiThreads], int etid) {
+    const int rounds = __reduce_max_sync(0xffffffffu, qlen);
+#pragma unroll 1
+    for (int t = 0; t < rounds; ++t) {
+        if (t < qlen) {
+            const float x = queue_v[t][etid];
+            if (x < worst) {
+                list_push<R>(ls, li, x, queue_i[t][etid]);
+                worst = ls[R - 1];
+            }
+        }
+    }
+    qlen = 0;
+    __syncwarp();
+}
+
+template <int R, bool kIP>
 __global__ void __launch_bounds__(kThreads, 1)
     knn_select_tc(const __grid_constant__ CUtensorMap tmap, const float *__restrict__ sqnorm,
-                  int64_t N, int ksteps, int katoms, int dist, int32_t *__restrict__ cand_i,
+                  int64_t N, int ksteps, int katoms, int32_t *__restrict__ cand_i,
                   int *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     SharedStorage &s = *reinterpret_cast<SharedStorage *>(
@@ -326,7 +380,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int quad = warp & 3;
         const int etid = threadIdx.x - kEpiWarp0 * 32;
         const int row_in_tile = h * 128 + quad * 32 + lane;
-        const bool l2 = (dist == kSquaredL2);
+        // Accumulator columns per tcgen05.ld: 32 for 32-entry lists and the
+        // inner-product scan; 16 where 64-entry lists or the squared-L2 norm
+        // terms leave fewer registers.
+        constexpr int kC = (R <= 32 && kIP) ? 32 : 16;
         uint32_t acc_phase = 0;
         int acc = 0;
         for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
@@ -340,6 +397,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 li[t] = -1;
             }
             float worst = FLT_MAX;
+            int qlen = 0;
             bool ok = true;
             for (int64_t ct = 0; ct < n_ct; ++ct) {
                 if (!mbar_wait(s, &s.acc_full[acc], acc_phase, err, 6)) {
@@ -350,20 +408,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int64_t c0 = ct * kCandTile;
                 const bool tail = c0 + kCandTile > N;
 #pragma unroll 1
-                for (int chunk = 0; chunk < kCandTile / kChunk; ++chunk) {
-                    float v[kChunk];
+                for (int chunk = 0; chunk < kCandTile / kC; ++chunk) {
+                    float v[kC];
                     __syncwarp();
-                    const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
-                                           (uint32_t)(acc * 256 + h * 128 + chunk * kChunk);
-                    tmem_ld16(taddr, v);
-                    tmem_wait_ld();
-                    const int64_t cb = c0 + chunk * kChunk;
-                    // Scores, lower is better: |c|^2 - 2<q,c> (squared L2) or -<q,c>.
-                    // The inner-product scan compares the raw maximum and negates
-                    // only the values it keeps.
-                    if (l2) {
+                    tmem_ld(tmem + ((uint32_t)(quad * 32) << 16) +
+                                (uint32_t)(acc * 256 + h * 128 + chunk * kC),
+                            v);
+                    const int64_t cb = c0 + chunk * kC;
+                    // Scores, lower is better: |c|^2 - 2<q,c> (squared L2) or
+                    // -<q,c> (kept as +<q,c>, compared against -worst).
+                    if constexpr (!kIP) {
 #pragma unroll
-                        for (int j = 0; j < kChunk; ++j) {
+                        for (int j = 0; j < kC; ++j) {
                             const int64_t c = cb + j;
                             const float nc = (c < N) ? __ldg(sqnorm + c) : 0.f;
                             v[j] = fmaf(-2.f, v[j], nc);
@@ -371,49 +427,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                     if (tail) {
 #pragma unroll
-                        for (int j = 0; j < kChunk; ++j)
-                            if (cb + j >= N) v[j] = l2 ? FLT_MAX : -FLT_MAX;
+                        for (int j = 0; j < kC; ++j)
+                            if (cb + j >= N) v[j] = kIP ? -FLT_MAX : FLT_MAX;
                     }
-                    float best;
-                    if (l2) {
-                        best = FLT_MAX;
-#pragma unroll
-                        for (int j = 0; j < kChunk; ++j) best = fminf(best, v[j]);
-                    } else {
-                        float top = -FLT_MAX;
-#pragma unroll
-                        for (int j = 0; j < kChunk; ++j) top = fmaxf(top, v[j]);
-                        best = -top;
-                        if (__any_sync(0xffffffffu, live && best < worst)) {
-#pragma unroll
-                            for (int j = 0; j < kChunk; ++j) v[j] = -v[j];
-                        }
-                    }
+                    const float best = kIP ? -tree_reduce<true, kC>(v) : tree_reduce<false, kC>(v);
                     const bool hit = live && best < worst;
-                    if (__any_sync(0xffffffffu, hit)) {
-                        // Each lane compacts its qualifying candidates (predicated
-                        // stores, no branches), then the warp inserts them in
-                        // lockstep: one round per slot of the fullest lane.
-                        int cnt = 0;
+                    if (!__any_sync(0xffffffffu, hit)) continue;
+                    // Qualifying candidates are queued (16 columns at a time);
+                    // a queue past half full is flushed into the lists first.
+#pragma unroll
+                    for (int half = 0; half < kC / 16; ++half) {
+                        if (__any_sync(0xffffffffu, qlen > kQueue - 16))
+                            flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
                         if (hit) {
 #pragma unroll
-                            for (int j = 0; j < kChunk; ++j) {
-                                const bool q = v[j] < worst;
-                                if (q) {
-                                    s.stage_v[cnt][etid] = v[j];
-                                    s.stage_i[cnt][etid] = (int32_t)(cb + j);
-                                }
-                                cnt += q ? 1 : 0;
-                            }
-                        }
-                        const int rounds = __reduce_max_sync(0xffffffffu, cnt);
-#pragma unroll 1
-                        for (int t = 0; t < rounds; ++t) {
-                            if (t < cnt) {
-                                const float x = s.stage_v[t][etid];
+                            for (int j = 0; j < 16; ++j) {
+                                const float x = kIP ? -v[half * 16 + j] : v[half * 16 + j];
                                 if (x < worst) {
-                                    list_push<R>(ls, li, x, s.stage_i[t][etid]);
-                                    worst = ls[R - 1];
+                                    s.queue_v[qlen][etid] = x;
+                                    s.queue_i[qlen][etid] = (int32_t)(cb + half * 16 + j);
+                                    ++qlen;
                                 }
                             }
                         }
@@ -426,6 +459,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (acc == 0) acc_phase ^= 1;
             }
             if (!ok) break;
+            flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
             if (live) {
 #pragma unroll
                 for (int t = 0; t < R; ++t) cand_i[grow * R + t] = li[t];
@@ -492,22 +526,19 @@ void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t 
     require(r == CUDA_SUCCESS, "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")",
             kCudaError);
     const size_t smem = sizeof(SharedStorage) + 1024;
-    static bool configured = false;
-    if (!configured) {
-        NCVIS_CUDA(cudaFuncSetAttribute(knn_select_tc<32>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_CUDA(cudaFuncSetAttribute(knn_select_tc<64>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
     const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
     const unsigned grid = (unsigned)std::min<int64_t>(n_qt, num_sms());
+    const bool ip = dist != kSquaredL2;
+    auto go = [&](auto kernel) {
+        NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms, cand_i,
+                     timeout_flag);
+    };
     if (plan.R == 32)
-        NCVIS_LAUNCH(knn_select_tc<32>, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms,
-                     dist, cand_i, timeout_flag);
+        ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);
     else
-        NCVIS_LAUNCH(knn_select_tc<64>, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms,
-                     dist, cand_i, timeout_flag);
+        ip ? go(knn_select_tc<64, true>) : go(knn_select_tc<64, false>);
 }
 
 }  // namespace ncvis_gpu

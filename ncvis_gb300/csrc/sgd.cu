@@ -144,18 +144,28 @@ template <int D>
 __device__ __forceinline__ void run_edge(float *Y, Vec<D> &yi, uint32_t i, uint32_t j, int64_t e,
                                          uint32_t N, uint32_t lo, const EpochConst &k, float &Qc,
                                          uint32_t key0, uint32_t key1, uint32_t tag) {
+    // Rows gathered per round trip: eight for D <= 3; four for D = 4, where
+    // eight 4-float rows in flight spill registers.
+    constexpr int kGroup = D <= 3 ? 8 : 4;
     int s = 0;  // next noise sample
     if (j != i) {
-        // The positive sample and the first noise pair share one group.
-        uint32_t o[3] = {j, 0u, 0u};
-        const int cnt = k.nu >= 2 ? 3 : 1 + k.nu;
-        if (k.nu >= 1) {
-            noise_pair(key0, key1, (uint64_t)e, tag, 0, i - lo, N, o[1], o[2]);
-            o[1] += lo;
-            o[2] += lo;
+        // The positive sample and the first kGroup - 2 noise samples share one
+        // group (one round trip per edge while nu <= kGroup - 2).
+        uint32_t o[kGroup - 1];
+        o[0] = j;
+        const int first = min(k.nu, kGroup - 2);
+#pragma unroll
+        for (int p = 0; p < kGroup / 2 - 1; ++p) {
+            o[1 + 2 * p] = o[2 + 2 * p] = 0u;
+            if (2 * p < first) {
+                noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)p, i - lo, N, o[1 + 2 * p],
+                           o[2 + 2 * p]);
+                o[1 + 2 * p] += lo;
+                o[2 + 2 * p] += lo;
+            }
         }
-        run_group<D, 3>(Y, yi, o, cnt, true, k, Qc);
-        s = cnt - 1;
+        run_group<D, kGroup - 1>(Y, yi, o, 1 + first, true, k, Qc);
+        s = first;
     } else {
         // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
         const float ws = nce_weight(0.f, true, k, Qc);
@@ -165,14 +175,17 @@ __device__ __forceinline__ void run_edge(float *Y, Vec<D> &yi, uint32_t i, uint3
             yi.v[c] = (yi.v[c] + dx) - dx;
         }
     }
-    // Remaining noise samples in groups of four (two Philox blocks each).
-    for (; s < k.nu; s += 4) {
-        uint32_t o[4];
-        noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1), i - lo, N, o[0], o[1]);
-        noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + 1, i - lo, N, o[2], o[3]);
+    // Remaining noise samples in groups of kGroup (kGroup / 2 Philox blocks).
+    for (; s < k.nu; s += kGroup) {
+        uint32_t o[kGroup];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) o[t] += lo;
-        run_group<D, 4>(Y, yi, o, min(4, k.nu - s), false, k, Qc);
+        for (int p = 0; p < kGroup / 2; ++p) {
+            noise_pair(key0, key1, (uint64_t)e, tag, (uint32_t)(s >> 1) + p, i - lo, N, o[2 * p],
+                       o[2 * p + 1]);
+            o[2 * p] += lo;
+            o[2 * p + 1] += lo;
+        }
+        run_group<D, kGroup>(Y, yi, o, min(kGroup, k.nu - s), false, k, Qc);
     }
 }
 
