@@ -14,8 +14,10 @@
 // thread is such a chain: a contiguous chunk of edges, a private Q copy, and
 // Philox4x32-10 noise keyed by (seed) and counted by (edge, epoch, sample
 // pair, retry); the chains' copies are averaged in FP64 by reduce_q.  Y is
-// read and written through L2 (ld/st.cg) so that chains on other SMs see each
-// other's updates as the reference's threads do.
+// read through L2 (ld.cg) so that chains on other SMs see each other's
+// updates as the reference's threads do; y_o -= dx is an L2 reduction
+// (red.add), y_i is kept in registers over a run of equal sources and
+// stored when the source changes.
 //
 // Replay mode (sgd_replay): one thread executes the one-thread reference
 // sample by sample, with the reference build's arithmetic grouping (noise
@@ -66,6 +68,28 @@ __device__ __forceinline__ void store_row(float *Y, int64_t i, const Vec<D> &r) 
     }
 }
 
+// y[row] -= dx as an L2 reduction: no read-modify-write round trip through
+// the SM, and concurrent updates of the row by other chains all land (plain
+// stores of 8-byte rows from many SMs contend for the same 32-byte sectors
+// and run at about half the rate).  With no concurrent writer the result is
+// the store of y - dx bit for bit.
+template <int D>
+__device__ __forceinline__ void sub_row(float *Y, int64_t i, const Vec<D> &dx) {
+    float *p = Y + i * D;
+    if constexpr (D == 2) {
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(-dx.v[0]), "f"(-dx.v[1])
+                     : "memory");
+    } else if constexpr (D == 4) {
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(-dx.v[0]),
+                     "f"(-dx.v[1]), "f"(-dx.v[2]), "f"(-dx.v[3])
+                     : "memory");
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c)
+            asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p + c), "f"(-dx.v[c]) : "memory");
+    }
+}
+
 struct EpochConst {
     float step, nu_f, a, b, ab, alpha_Q, pow_b1_at_zero;
     int nu;
@@ -106,17 +130,6 @@ __device__ __forceinline__ float sq_dist(const Vec<D> &x, const Vec<D> &y) {
 
 __device__ __forceinline__ float clip4(float v) { return fminf(fmaxf(v, -4.f), 4.f); }
 
-// y_i += dx, y_o -= dx on distinct rows.
-template <int D>
-__device__ __forceinline__ void apply(Vec<D> &yi, Vec<D> &yo, float ws) {
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-        const float dx = clip4((yo.v[c] - yi.v[c]) * ws);
-        yi.v[c] += dx;
-        yo.v[c] -= dx;
-    }
-}
-
 // Samples of a group whose row was loaded before an earlier sample of the
 // same group stored it are reloaded, so a chain always sees its own updates.
 template <int D, int G>
@@ -133,8 +146,14 @@ __device__ __forceinline__ void run_group(float *Y, Vec<D> &yi, const uint32_t (
 #pragma unroll
         for (int u = 0; u < t; ++u) dup |= (o[u] == o[t]);
         if (dup) yo[t] = load_row<D>(Y, o[t]);
-        apply<D>(yi, yo[t], nce_weight(sq_dist<D>(yi, yo[t]), first_is_positive && t == 0, k, Qc));
-        store_row<D>(Y, o[t], yo[t]);
+        const float ws = nce_weight(sq_dist<D>(yi, yo[t]), first_is_positive && t == 0, k, Qc);
+        Vec<D> dx;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            dx.v[c] = clip4((yo[t].v[c] - yi.v[c]) * ws);
+            yi.v[c] += dx.v[c];
+        }
+        sub_row<D>(Y, o[t], dx);
     }
 }
 

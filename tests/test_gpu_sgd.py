@@ -123,6 +123,44 @@ def test_hogwild_invariants(cuda, oracle, d):
     assert 0.5 < np.std(Y) / np.std(Yr) < 2.0
 
 
+@pytest.mark.parametrize("d", [1, 2, 3, 4])
+def test_grouped_chain_matches_sequential_chain(cuda, d):
+    """One chain, so the result is deterministic: the kernel for d <= 4, which
+    gathers the rows of a group of samples before applying them, keeps y_i in
+    registers across a run of equal sources and applies y_o -= dx as an L2
+    reduction, must give bit-identical Y and Q to the plain kernel for d > 4,
+    which reads and stores every row when it is used; the latter runs on the
+    same embedding padded with zero columns to d = 5 (zero columns add exact
+    zeros to every distance and never move).  Small N and up to 20 noise
+    samples per edge make samples of one group hit the same row all the time;
+    runs of 1-5 equal sources and self edges cover the write-back of y_i."""
+    from ncvis_gb300 import stages
+    rng = np.random.default_rng(d)
+    N = 24
+    runs = rng.integers(1, 6, size=60)
+    src = np.repeat(rng.integers(0, N, size=runs.size), runs).astype(np.int32)
+    dst = rng.integers(0, N, size=src.size).astype(np.int32)
+    self_edges = rng.random(src.size) < 0.05
+    dst[self_edges] = src[self_edges]
+    plan = np.array([0, 1, 2, 3, 7, 20], dtype=np.uint64)
+    Y0 = rng.normal(0, 1, size=(N, d)).astype(np.float32)
+    Y5 = np.zeros((N, 5), np.float32)
+    Y5[:, :d] = Y0
+    out = []
+    for Y in (Y0, Y5):
+        dY = _t(cuda, Y, np.float32)
+        dQ = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+        stages.optimize(dY, dQ, _t(cuda, src, np.int32), _t(cuda, dst, np.int32), 7, plan, A, B,
+                        chains=1)
+        out.append((dY.cpu().numpy(), float(dQ.cpu()[0])))
+    (Yw, Qw), (Ys, Qs) = out
+    assert np.isfinite(Yw).all()
+    assert not np.array_equal(Yw, Y0)
+    assert np.array_equal(Ys[:, d:], np.zeros((N, 5 - d), np.float32))
+    assert np.array_equal(Yw.view(np.uint32), Ys[:, :d].copy().view(np.uint32))
+    assert np.float32(Qw).view(np.uint32) == np.float32(Qs).view(np.uint32)
+
+
 def test_hogwild_rejects_bad_edges(cuda):
     from ncvis_gb300 import NcvisError, stages
     dY = cuda.zeros((10, 2), dtype=cuda.float32, device="cuda")
