@@ -235,6 +235,21 @@ def recall_at_15(X, inds, n_queries=2000, seed=0):
     return hits / (n_queries * K_NN)
 
 
+def update_ceiling(rows, rate):
+    """The GPU's rate for the optimizer's per-sample traffic (a random row
+    gather plus a random row reduction over an L2-resident array of `rows`
+    2-float rows), measured live, and the SGD's pair-update rate as a
+    fraction of it."""
+    import ctypes as C
+    from ncvis_gb300 import _lib
+    g, u = C.c_double(0), C.c_double(0)
+    rc = _lib.lib().ncvis_measure_update_rate(rows, D_EMB, C.byref(g), C.byref(u), None)
+    if rc != 0:
+        return {"update_ceiling_error": _lib.lib().ncvis_get_last_error().decode()}
+    return {"gather_ceiling_per_s": g.value, "update_ceiling_per_s": u.value,
+            "frac_of_update_ceiling": rate / u.value}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -366,6 +381,7 @@ def run_ours(args):
         "sgd": {"pair_updates_per_s": pair_updates / (opt_ms / 1000.0),
                 "edge_epochs_per_s": E * EPOCHS / (opt_ms / 1000.0), "optimize_ms": opt_ms,
                 "algorithmic_GBps": sgd_gbs, "hbm_peak_GBps": hbm, "frac_of_hbm": sgd_gbs / hbm,
+                **update_ceiling(n, pair_updates / (opt_ms / 1000.0)),
                 "E": E},
         "recall_at_15": recall,
         "quality": quality,

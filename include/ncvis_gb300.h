@@ -223,6 +223,17 @@ int ncvis_nce_loss_device_noalloc(size_t N, size_t d, size_t E, const int32_t *d
                                   size_t n_noise, float a, float b, uint64_t seed, uint32_t tag,
                                   uint64_t edge_offset, double *d_loss, void *stream);
 
+/* Diagnostic: the rate at which this GPU serves the optimizer's memory
+ * pattern, the ceiling for ncvis_optimize_device's pair-update rate.  On the
+ * optimizer's launch shape it times random row gathers over a zeroed array of
+ * `rows` rows of d floats (d = 1, 2 or 4), and random row gathers each followed
+ * by a reduction into the same row (the optimizer's per-sample traffic):
+ * *gathers_per_s and *updates_per_s.  Allocates and frees the array; runs on
+ * `stream` and waits for it.  No counterpart in the reference (an addition).
+ * Errors: ncvis_get_last_error(). */
+int ncvis_measure_update_rate(size_t rows, size_t d, double *gathers_per_s, double *updates_per_s,
+                              void *stream);
+
 /* Number of kernels this library has launched in the process so far. */
 uint64_t ncvis_kernel_launch_count(void);
 

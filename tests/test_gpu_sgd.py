@@ -169,3 +169,18 @@ def test_hogwild_rejects_bad_edges(cuda):
     dst = cuda.tensor([1, 2, 10], dtype=cuda.int32, device="cuda")
     with pytest.raises(NcvisError, match="outside"):
         stages.optimize(dY, dQ, src, dst, 1, np.array([1], np.uintp), A, B)
+
+
+def test_update_rate_diagnostic(cuda):
+    """The optimizer's ceiling probe: random row gathers and random gathers
+    plus reductions over a 2^20-row array both report positive rates, the
+    update rate is not above the gather rate, and unsupported row widths are
+    refused."""
+    import ctypes as C
+    from ncvis_gb300 import _lib
+    L = _lib.lib()
+    g, u = C.c_double(0), C.c_double(0)
+    assert L.ncvis_measure_update_rate(1 << 20, 2, C.byref(g), C.byref(u), None) == 0
+    assert 1e8 < u.value <= 1.1 * g.value
+    assert L.ncvis_measure_update_rate(1 << 20, 3, C.byref(g), C.byref(u), None) == 3
+    assert b"d must be 1, 2 or 4" in L.ncvis_get_last_error()
