@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 
 N_FULL, D_FULL, K_NN, D_EMB, EPOCHS, INIT_EPOCHS = 1_024_000, 100, 15, 2, 50, 20
 SAMPLE_N = 65_536  # CPU-baseline sample of the same generator
+# DRAM bytes (read + write) of one full-size BF16 kNN-selection launch, from the
+# ncu capture in profiles/knn_select_tc_1024000x100_dram.md.
+KNN_TRAFFIC_BYTES = 6.80e9
 
 
 def parse():
@@ -328,7 +331,9 @@ def run_ours(args):
                 "peak_source": "nominal FP32 FFMA (152 SMs x 128 lanes x 2 flop x 2.07 GHz)"}
     achieved = flops / (knn_ms / 1000.0) / 1e12
     roof.update({"kernel": "knn candidate selection", "achieved": achieved, "peak": peak,
-                 "frac": achieved / peak, "traffic": None,
+                 "frac": achieved / peak,
+                 "traffic": KNN_TRAFFIC_BYTES if (n == N_FULL and args.knn == "bf16") else None,
+                 "traffic_unit": "DRAM bytes per launch (ncu)",
                  "algorithmic": f"2*N^2*D = {flops:.3e} FLOP per launch (D=100 unpadded)"})
     sgd_bytes = E * (EPOCHS * 4 + 16 * D_EMB * int((plan + 1).sum()))
     sgd_gbs = sgd_bytes / (opt_ms / 1000.0) / 1e9
