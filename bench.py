@@ -348,8 +348,9 @@ def run_ours(args):
     quality = None
     if not args.no_quality:
         # Embedding quality at k=15 of this path and of the plain FP32 path
-        # (one extra fit): kNN preservation on all points (exact kNN of X and
-        # of Y on the GPU) and trustworthiness on a 10,000-point sample.
+        # (one extra fit): kNN preservation and trustworthiness on all points
+        # (exact kNN of X and of Y, and every neighbour's rank, on the GPU),
+        # and trustworthiness of a 10,000-point sample by FP64 brute force.
         from ncvis_gb300 import quality as Qm
         Y_ours = vis.fit_transform(Xd)
         plain = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
@@ -364,6 +365,9 @@ def run_ours(args):
             "knn_preservation_full": {
                 "this_path": Qm.knn_preservation_device(Xd, Y_ours, K_NN, 2, x_inds=x_inds),
                 "plain_fp32_path": Qm.knn_preservation_device(Xd, Y_plain, K_NN, 2, x_inds=x_inds)},
+            "trustworthiness_full": {
+                "this_path": Qm.trustworthiness_device(Xd, Y_ours, K_NN, distance=2),
+                "plain_fp32_path": Qm.trustworthiness_device(Xd, Y_plain, K_NN, distance=2)},
             "trustworthiness_sample10k": {
                 "this_path": Qm.trustworthiness(Xs, Y_ours[sub].cpu().numpy(), K_NN),
                 "plain_fp32_path": Qm.trustworthiness(Xs, Y_plain[sub].cpu().numpy(), K_NN)},

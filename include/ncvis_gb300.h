@@ -223,6 +223,19 @@ int ncvis_nce_loss_device_noalloc(size_t N, size_t d, size_t E, const int32_t *d
                                   size_t n_noise, float a, float b, uint64_t seed, uint32_t tag,
                                   uint64_t edge_offset, double *d_loss, void *stream);
 
+/* Trustworthiness at k (Venna & Kaski 2001, as scikit-learn's
+ * manifold.trustworthiness defines it) of the embedding dY [N, d] of dX
+ * [N, D] (device float32, row-major), at full size: the embedding's exact kNN
+ * (squared L2), then for every point the rank in X, under `distance` (the
+ * engine's distances after its preprocessing), of each embedding neighbour,
+ * counted over all N points in one FP32 pass.  1 <= k <= 16, 2k + 2 <= N.
+ * *out receives T(k).  Allocates its scratch on `stream`; waits for it.
+ * Replaces the reference's (and the tests') subsampled CPU check; no
+ * counterpart in the reference's code (an addition).  Errors:
+ * ncvis_get_last_error(). */
+int ncvis_trustworthiness_device(const float *dX, size_t N, size_t D, int distance,
+                                 const float *dY, size_t d, size_t k, double *out, void *stream);
+
 /* Diagnostic: the rate at which this GPU serves the optimizer's memory
  * pattern, the ceiling for ncvis_optimize_device's pair-update rate.  On the
  * optimizer's launch shape it times random row gathers over a zeroed array of

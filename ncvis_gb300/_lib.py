@@ -121,6 +121,9 @@ SIGNATURES = {
     "ncvis_nce_loss_device_noalloc": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, _sz,
                                                 C.c_float, C.c_float, C.c_uint64, C.c_uint32,
                                                 C.c_uint64, _vp, _vp]),
+    "ncvis_trustworthiness_device": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_int,
+                                               C.c_void_p, C.c_size_t, C.c_size_t,
+                                               C.POINTER(C.c_double), C.c_void_p]),
     "ncvis_measure_update_rate": (C.c_int, [C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.c_void_p]),
     "ncvis_kernel_launch_count": (C.c_uint64, []),

@@ -101,6 +101,24 @@ def knn_preservation_device(X, Y, k: int = 15, distance: int = 0, x_inds=None) -
     return hits / (a.shape[0] * k)
 
 
+def trustworthiness_device(X, Y, k: int = 15, distance: int = 0) -> float:
+    """Trustworthiness at k over all N points on the GPU (the engine's
+    ncvis_trustworthiness_device): the embedding's exact kNN, then each
+    neighbour's rank in X under the engine's `distance` (0 squared L2,
+    1 inner product, 2 cosine, 3 correlation; for unit vectors the cosine
+    ranks are the Euclidean ranks), counted over all points."""
+    import ctypes as C
+    from . import _lib, stages
+    torch = _torch()
+    Xd = _as_tensor(X, "cuda").contiguous()
+    Yd = _as_tensor(Y, "cuda").contiguous()
+    out = C.c_double(0.0)
+    _lib.check(_lib.lib().ncvis_trustworthiness_device(
+        Xd.data_ptr(), Xd.shape[0], Xd.shape[1], distance, Yd.data_ptr(), Yd.shape[1], k,
+        C.byref(out), stages._stream()))
+    return out.value
+
+
 def recall_at_k(found, exact) -> float:
     """Mean fraction of each row of `exact` (index sets) present in `found`."""
     found = np.asarray(found)
