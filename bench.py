@@ -355,13 +355,24 @@ def run_ours(args):
         Y_ours = vis.fit_transform(Xd)
         plain = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
                             random_seed=42, distance="cosine", knn_precision="fp32")
+        plain.fit_transform(Xd)  # warm-up (arena, kernels)
+        torch.cuda.synchronize()
+        t_plain = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_plain[0].record()
         Y_plain = plain.fit_transform(Xd)
+        t_plain[1].record()
+        torch.cuda.synchronize()
+        plain_s = t_plain[0].elapsed_time(t_plain[1]) / 1000.0
+        plain_stages = plain.stage_times()
         # X's table: the one measured above against FP64 (recall_at_15), else exact FP32.
         x_inds = inds if inds is not None else stages.knn(Xd, K_NN, 2, precision=0)[0]
         sub = np.sort(np.random.default_rng(1).choice(n, min(n, 10000), replace=False))
         Xs = X[sub] / np.linalg.norm(X[sub], axis=1, keepdims=True)
         quality = {
             "k": K_NN,
+            "plain_fp32_path_fit_s": plain_s,
+            "plain_fp32_path_knn_ms": plain_stages["knn_ms"],
+            "speedup_vs_plain_fp32_path": plain_s / step_s,
             "knn_preservation_full": {
                 "this_path": Qm.knn_preservation_device(Xd, Y_ours, K_NN, 2, x_inds=x_inds),
                 "plain_fp32_path": Qm.knn_preservation_device(Xd, Y_plain, K_NN, 2, x_inds=x_inds)},
