@@ -795,8 +795,7 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
                 "optimize: need 0 <= epoch_begin <= epoch_end <= n_epochs");
         cudaStream_t s = (cudaStream_t)stream;
         if (E == 0 || epoch_begin == epoch_end) return;
-        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
-                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+        require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "optimize: an edge endpoint is outside [0, N)");
         if (chains <= 0) chains = sgd_default_chains((int64_t)E, (int64_t)N, (int)d);
         void *ws = nullptr;
@@ -844,8 +843,7 @@ int ncvis_nce_loss_device(size_t N, size_t d, size_t E, const int32_t *d_src, co
                     n_noise <= 1024,
                 "nce_loss: need 2 <= N < 2^31, 1 <= d <= 32, 1 <= n_noise <= 1024");
         cudaStream_t s = (cudaStream_t)stream;
-        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
-                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+        require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "nce_loss: an edge endpoint is outside [0, N)");
         void *ws = nullptr;
         NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));
@@ -866,8 +864,7 @@ int ncvis_nce_grad_device(size_t N, size_t d, size_t E, const int32_t *d_src, co
                     n_noise <= 1024,
                 "nce_grad: need 2 <= N < 2^31, 1 <= d <= 32, 1 <= n_noise <= 1024");
         cudaStream_t s = (cudaStream_t)stream;
-        require(indices_in_range(d_src, (int64_t)E, (int64_t)N, s) &&
-                    indices_in_range(d_dst, (int64_t)E, (int64_t)N, s),
+        require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "nce_grad: an edge endpoint is outside [0, N)");
         void *ws = nullptr;
         NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));

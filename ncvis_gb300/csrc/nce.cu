@@ -42,22 +42,19 @@ struct NceConst {
 };
 
 // Terms of one sample: loss, dL/dQ (w) and g (dL/dy_i = g (y_i - y_o)).
+// d2^(b-1) is d2^b / d2; softplus and the sigmoid share exp(-|u|).
 __device__ __forceinline__ void sample_terms(float d2, bool positive, const NceConst &c,
                                              float &loss, float &w, float &g) {
     const float p = d2 > 0.f ? powf(d2, c.b) : 0.f;
-    const float p1 = d2 > 0.f ? powf(d2, c.b - 1.f) : c.pow_b1_at_zero;
-    const float log_ph = -log1pf(c.a * p);
-    const float ph = 1.f / (1.f + c.a * p);
-    float u;
-    if (positive) {
-        u = c.log_nu + c.Q - log_ph;
-        loss = softplus(u);
-        w = sigmoid(u);
-    } else {
-        u = log_ph - c.Q - c.log_nu;
-        loss = softplus(u);
-        w = -sigmoid(u);
-    }
+    const float p1 = d2 > 0.f ? p / d2 : c.pow_b1_at_zero;
+    const float ap = c.a * p;
+    const float log_ph = -log1pf(ap);
+    const float ph = 1.f / (1.f + ap);
+    const float u = positive ? c.log_nu + c.Q - log_ph : log_ph - c.Q - c.log_nu;
+    const float t = __expf(-fabsf(u));
+    loss = fmaxf(u, 0.f) + log1pf(t);
+    const float sg = u >= 0.f ? 1.f / (1.f + t) : t / (1.f + t);
+    w = positive ? sg : -sg;
     g = 2.f * w * c.a * c.b * ph * p1;
 }
 
@@ -124,6 +121,114 @@ __global__ void __launch_bounds__(kThreads) nce_edges(int mode, int64_t E, int d
     block_sum2(acc_loss, acc_dq, part);
 }
 
+template <int D>
+struct Row {
+    float v[D];
+};
+
+template <int D>
+__device__ __forceinline__ Row<D> load_row(const float *__restrict__ Y, int64_t i) {
+    Row<D> r;
+    const float *p = Y + i * D;
+    if constexpr (D % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < D; q += 4) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(p + q));
+            r.v[q] = t.x, r.v[q + 1] = t.y, r.v[q + 2] = t.z, r.v[q + 3] = t.w;
+        }
+    } else if constexpr (D == 2) {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+        r.v[0] = t.x, r.v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q) r.v[q] = __ldg(p + q);
+    }
+    return r;
+}
+
+// dY[i] += g as L2 vector reductions.
+template <int D>
+__device__ __forceinline__ void add_row(float *dY, int64_t i, const Row<D> &g) {
+    float *p = dY + i * D;
+    if constexpr (D % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < D; q += 4)
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p + q),
+                         "f"(g.v[q]), "f"(g.v[q + 1]), "f"(g.v[q + 2]), "f"(g.v[q + 3])
+                         : "memory");
+    } else if constexpr (D == 2) {
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(g.v[0]), "f"(g.v[1])
+                     : "memory");
+    } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q) atomicAdd(p + q, g.v[q]);
+    }
+}
+
+// nce_edges for d = D with rows of 4 D bytes aligned to their vector width:
+// y_i read once per edge and its gradient summed in registers, noise drawn
+// two samples per Philox block (the same indices as noise_index), the y_o
+// gradients applied as L2 reductions, per-thread sums in FP32 (1 + nu terms)
+// and the block sums in FP64.
+template <int D>
+__global__ void __launch_bounds__(kThreads) nce_edges_t(int mode, int64_t E, uint32_t N,
+                                                        const int32_t *__restrict__ src,
+                                                        const int32_t *__restrict__ dst,
+                                                        const float *__restrict__ Y,
+                                                        const float *__restrict__ Qp,
+                                                        uint64_t edge_offset, NceConst c,
+                                                        const float *__restrict__ scale,
+                                                        float *__restrict__ dY,
+                                                        double *__restrict__ part) {
+    const int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    c.Q = *Qp;
+    float acc_loss = 0.f, acc_dq = 0.f;
+    if (e < E) {
+        const int64_t i = src[e];
+        const Row<D> yi = load_row<D>(Y, i);
+        const float sc = (mode == 1) ? *scale : 0.f;
+        Row<D> gi;
+#pragma unroll
+        for (int q = 0; q < D; ++q) gi.v[q] = 0.f;
+        uint32_t second = 0;
+        for (int s = 0; s <= c.nu; ++s) {
+            uint32_t o;
+            if (s == 0) {
+                o = (uint32_t)dst[e];
+            } else if (((s - 1) & 1) == 0) {
+                noise_pair(c.k0, c.k1, edge_offset + (uint64_t)e, c.tag, (uint32_t)(s - 1) >> 1,
+                           (uint32_t)i, N, o, second);
+            } else {
+                o = second;
+            }
+            const Row<D> yo = load_row<D>(Y, o);
+            Row<D> diff;
+            float d2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                diff.v[q] = yi.v[q] - yo.v[q];
+                d2 = fmaf(diff.v[q], diff.v[q], d2);
+            }
+            float loss, w, g;
+            sample_terms(d2, s == 0, c, loss, w, g);
+            acc_loss += loss;
+            acc_dq += w;
+            if (mode == 1 && (int64_t)o != i) {
+                const float gs = g * sc;
+                Row<D> go;
+#pragma unroll
+                for (int q = 0; q < D; ++q) {
+                    gi.v[q] = fmaf(gs, diff.v[q], gi.v[q]);
+                    go.v[q] = -gs * diff.v[q];
+                }
+                add_row<D>(dY, o, go);
+            }
+        }
+        if (mode == 1) add_row<D>(dY, i, gi);
+    }
+    block_sum2((double)acc_loss, (double)acc_dq, part);
+}
+
 // out[0] = sum of part[2b + which] over blocks (FP64), optionally scaled.
 __global__ void finish_sum(const double *__restrict__ part, int blocks, int which,
                            const float *__restrict__ scale, double *__restrict__ out) {
@@ -181,8 +286,26 @@ void run_nce(int mode, int64_t N, int d, int64_t E, const int32_t *src, const in
     c.tag = tag;
     const int blocks = (int)std::max<int64_t>((E + kThreads - 1) / kThreads, 1);
     double *part = (double *)workspace;
-    NCVIS_LAUNCH(nce_edges, blocks, kThreads, 0, s, mode, E, d, (uint32_t)N, src, dst, Y, Q,
-                 edge_offset, c, scale, dY, part);
+    // Templated kernels where a row's vector loads and reductions are aligned.
+    const uintptr_t rows = (uintptr_t)Y | (uintptr_t)(mode == 1 ? dY : Y);
+    const bool v2 = (rows & 7) == 0, v4 = (rows & 15) == 0;
+#define NCE_T(DD)                                                                                 \
+    NCVIS_LAUNCH(nce_edges_t<DD>, blocks, kThreads, 0, s, mode, E, (uint32_t)N, src, dst, Y, Q, \
+                 edge_offset, c, scale, dY, part)
+    if (d == 1)
+        NCE_T(1);
+    else if (d == 2 && v2)
+        NCE_T(2);
+    else if (d == 4 && v4)
+        NCE_T(4);
+    else if (d == 8 && v4)
+        NCE_T(8);
+    else if (d == 16 && v4)
+        NCE_T(16);
+    else
+        NCVIS_LAUNCH(nce_edges, blocks, kThreads, 0, s, mode, E, d, (uint32_t)N, src, dst, Y, Q,
+                     edge_offset, c, scale, dY, part);
+#undef NCE_T
     NCVIS_LAUNCH(finish_sum, 1, 1024, 0, s, part, blocks, mode == 0 ? 0 : 1,
                  mode == 0 ? nullptr : scale, out);
 }

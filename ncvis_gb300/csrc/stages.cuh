@@ -66,6 +66,7 @@ int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists
 
 // True when every a[0..n) lies in [0, N) (waits on the stream).
 bool indices_in_range(const int32_t *a, int64_t n, int64_t N, cudaStream_t s);
+bool edges_in_range(const int32_t *a, const int32_t *b, int64_t n, int64_t N, cudaStream_t s);
 
 // ---- device-wide exclusive scan ----------------------------------------------
 size_t scan_workspace_bytes(int64_t n);

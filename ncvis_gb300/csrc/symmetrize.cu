@@ -44,6 +44,17 @@ __global__ void check_indices(const int32_t *__restrict__ inds, int64_t nk, int6
     }
 }
 
+// bad = 1 if any entry of a or b (n each; b may be null) lies outside [0, N).
+__global__ void check_pairs(const int32_t *__restrict__ a, const int32_t *__restrict__ b,
+                            int64_t n, int64_t N, int *__restrict__ bad) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t t = a[e];
+        const int32_t u = b ? b[e] : 0;
+        if (t < 0 || t >= N || u < 0 || u >= N) atomicOr(bad, 1);
+    }
+}
+
 __global__ void count_targets(const int32_t *__restrict__ inds, int64_t nk,
                               int32_t *__restrict__ indeg) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk;
@@ -211,12 +222,17 @@ SymWs carve(void *ws, int64_t N, int k) {
 }  // namespace
 
 bool indices_in_range(const int32_t *a, int64_t n, int64_t N, cudaStream_t s) {
+    return edges_in_range(a, nullptr, n, N, s);
+}
+
+// One check kernel over both arrays and one wait for its flag.
+bool edges_in_range(const int32_t *a, const int32_t *b, int64_t n, int64_t N, cudaStream_t s) {
     if (n == 0) return true;
     int *bad = nullptr;
     NCVIS_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), s));
     NCVIS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
     const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 16 * num_sms());
-    NCVIS_LAUNCH(check_indices, grid, 256, 0, s, a, n, N, bad);
+    NCVIS_LAUNCH(check_pairs, grid, 256, 0, s, a, b, n, N, bad);
     int h = 0;
     NCVIS_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
     NCVIS_CUDA(cudaFreeAsync(bad, s));
