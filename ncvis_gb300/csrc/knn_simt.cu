@@ -31,14 +31,16 @@ constexpr int BM = 64;   // queries per block
 constexpr int BN = 128;  // candidates per tile
 constexpr int BK = 16;   // reduction slice
 constexpr int NT = 256;  // threads per block
+constexpr int AS = BM + 4;  // shared-memory row strides (float4-aligned, fewer bank conflicts)
+constexpr int BS = BN + 4;
 
 __device__ __forceinline__ bool pair_less(float da, int ia, float db, int ib) {
     return da < db || (da == db && ia < ib);
 }
 
 struct SelectSmem {
-    float *As;     // [BK][BM]
-    float *Bs;     // [BK][BN]
+    float *As;     // [BK][AS]
+    float *Bs;     // [BK][BS]
     float *lst_d;  // [R][BM]
     int *lst_i;    // [R][BM]
     float *buf_d;  // [BN][BM]
@@ -49,7 +51,7 @@ struct SelectSmem {
 };
 
 __host__ __device__ inline size_t select_smem_bytes(int R) {
-    return sizeof(float) * (BK * BM + BK * BN) + (sizeof(float) + sizeof(int)) * (size_t)R * BM +
+    return sizeof(float) * (BK * AS + BK * BS) + (sizeof(float) + sizeof(int)) * (size_t)R * BM +
            (sizeof(float) + sizeof(int)) * (size_t)BN * BM + sizeof(int) * 2 * BM +
            sizeof(float) * BM;
 }
@@ -57,8 +59,8 @@ __host__ __device__ inline size_t select_smem_bytes(int R) {
 __device__ inline SelectSmem carve(char *base, int R) {
     SelectSmem s;
     s.As = (float *)base;
-    s.Bs = s.As + BK * BM;
-    s.lst_d = s.Bs + BK * BN;
+    s.Bs = s.As + BK * AS;
+    s.lst_d = s.Bs + BK * BS;
     s.lst_i = (int *)(s.lst_d + R * BM);
     s.buf_d = (float *)(s.lst_i + R * BM);
     s.buf_i = (int *)(s.buf_d + BN * BM);
@@ -107,6 +109,28 @@ __global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ X
     }
     __syncthreads();
 
+    // Global -> register staging of one K slice: thread t holds the 4 values
+    // (k0 + 4 (t & 3) ..) of query row t / 4 and of candidate rows t / 4 and
+    // t / 4 + 64 (float4 loads when D is a multiple of 4).
+    const bool vec = (D & 3) == 0;
+    const int lr = tid >> 2, lk = (tid & 3) * 4;
+    auto load4 = [&](int64_t row, int64_t row_end, int kc, float4 &v) {
+        if (row < row_end && vec && kc < D) {
+            v = __ldg(reinterpret_cast<const float4 *>(Xp + row * D + kc));
+        } else {
+            v.x = (row < row_end && kc < D) ? Xp[row * D + kc] : 0.f;
+            v.y = (row < row_end && kc + 1 < D) ? Xp[row * D + kc + 1] : 0.f;
+            v.z = (row < row_end && kc + 2 < D) ? Xp[row * D + kc + 2] : 0.f;
+            v.w = (row < row_end && kc + 3 < D) ? Xp[row * D + kc + 3] : 0.f;
+        }
+    };
+    auto store4 = [&](float *M, int stride, int row, const float4 &v) {
+        M[(lk + 0) * stride + row] = v.x;
+        M[(lk + 1) * stride + row] = v.y;
+        M[(lk + 2) * stride + row] = v.z;
+        M[(lk + 3) * stride + row] = v.w;
+    };
+
     for (int64_t c0 = c_begin; c0 < c_end; c0 += BN) {
         float acc[4][8];
 #pragma unroll
@@ -114,32 +138,26 @@ __global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ X
 #pragma unroll
             for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
+        float4 ra, rb0, rb1;
+        load4(q0 + lr, N, lk, ra);
+        load4(c0 + lr, c_end, lk, rb0);
+        load4(c0 + 64 + lr, c_end, lk, rb1);
         for (int k0 = 0; k0 < D; k0 += BK) {
-            {  // queries: 64 rows x 16 columns, 4 per thread
-                const int q = tid >> 2, kk = (tid & 3) * 4;
-                const int64_t gq = q0 + q;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int kc = k0 + kk + j;
-                    sm.As[(kk + j) * BM + q] = (gq < N && kc < D) ? Xp[gq * D + kc] : 0.f;
-                }
-            }
-            {  // candidates: 128 rows x 16 columns, 8 per thread
-                const int c = tid >> 1, kk = (tid & 1) * 8;
-                const int64_t gc = c0 + c;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int kc = k0 + kk + j;
-                    sm.Bs[(kk + j) * BN + c] = (gc < c_end && kc < D) ? Xp[gc * D + kc] : 0.f;
-                }
-            }
+            store4(sm.As, AS, lr, ra);
+            store4(sm.Bs, BS, lr, rb0);
+            store4(sm.Bs, BS, lr + 64, rb1);
             __syncthreads();
+            if (k0 + BK < D) {  // next slice in flight while this one is used
+                load4(q0 + lr, N, k0 + BK + lk, ra);
+                load4(c0 + lr, c_end, k0 + BK + lk, rb0);
+                load4(c0 + 64 + lr, c_end, k0 + BK + lk, rb1);
+            }
 #pragma unroll
             for (int kk = 0; kk < BK; ++kk) {
-                const float4 a = *reinterpret_cast<const float4 *>(&sm.As[kk * BM + ty * 4]);
-                float b[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) b[j] = sm.Bs[kk * BN + tx + 16 * j];
+                const float4 a = *reinterpret_cast<const float4 *>(&sm.As[kk * AS + ty * 4]);
+                const float4 b0 = *reinterpret_cast<const float4 *>(&sm.Bs[kk * BS + tx * 4]);
+                const float4 b1 = *reinterpret_cast<const float4 *>(&sm.Bs[kk * BS + 64 + tx * 4]);
+                const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     acc[0][j] = fmaf(a.x, b[j], acc[0][j]);
@@ -154,7 +172,7 @@ __global__ void __launch_bounds__(NT) knn_select_f32(const float *__restrict__ X
         // Threshold filter into the per-query buffers.
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int64_t gc = c0 + tx + 16 * j;
+            const int64_t gc = c0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
             if (gc >= c_end) continue;
             const float cn = l2 ? sqnorm[gc] : 0.f;
 #pragma unroll
