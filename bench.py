@@ -483,7 +483,7 @@ def run_batched(args):
     Xs = [torch.from_numpy(gaussian_mixture(int(n), 64, int(rng.integers(4, 21)), 5.0, 1.0,
                                             seed=42 + p)[0]).to(dev) for p, n in enumerate(sizes)]
     seeds = list(range(42, 42 + len(Xs)))
-    vis = ncvis.NCVis(random_seed=42)
+    vis = ncvis.NCVis(random_seed=42, knn_precision=args.knn)
     for _ in range(args.warmup):
         vis.fit_transform_batched(Xs, seeds=seeds)
     torch.cuda.synchronize()
@@ -505,7 +505,10 @@ def run_batched(args):
                       "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
                       "data": "synthetic (seeded Gaussian mixtures)",
                       "config": {"workload": "256 embeddings, N log-uniform [500, 50000], D=64, "
-                                             "k=15, d=2, 50 epochs", "total_N": int(sizes.sum())},
+                                             "k=15, d=2, 50 epochs", "total_N": int(sizes.sum()),
+                                 "knn": ("BF16 tcgen05 + exact FP32 rerank" if args.knn == "bf16"
+                                         else "exact FP32"),
+                                 "loop": "plain per-problem path (exact FP32 kNN), one fit each"},
                       "wall_s": wall, "stage_ms": st, "loop_of_single_fits_s": loop,
                       "loop_pair_updates_per_s": updates / loop, "speedup_vs_loop": loop / wall}),
           flush=True)

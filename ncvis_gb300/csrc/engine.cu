@@ -123,11 +123,74 @@ __global__ void gather_offsets(const int64_t *__restrict__ row_ptr,
     if (p <= B) eoff[p] = row_ptr[off[p]];
 }
 
+// Copies each problem's BF16 rows and squared norms to its 256-aligned place
+// in the padded layout (problem p starts at row pad[p]); one warp per row.
+__global__ void pad_rows(const __nv_bfloat16 *__restrict__ Xb, const float *__restrict__ sqn,
+                         const int64_t *__restrict__ off, const int64_t *__restrict__ pad, int B,
+                         int64_t total, int ldb, __nv_bfloat16 *__restrict__ Xb_pad,
+                         float *__restrict__ sqn_pad) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= total) return;
+    const int p = segment_of(off, B, row);
+    const int64_t prow = pad[p] + (row - off[p]);
+    const uint16_t *src = reinterpret_cast<const uint16_t *>(Xb + row * ldb);
+    uint16_t *dst = reinterpret_cast<uint16_t *>(Xb_pad + prow * ldb);
+    for (int c = lane; c < ldb; c += 32) dst[c] = src[c];
+    if (lane == 0) sqn_pad[prow] = sqn[row];
+}
+
 }  // namespace
 
 }  // namespace ncvis_gpu
 
 using namespace ncvis_gpu;
+
+// Query tiles of the problems for one tensor-core launch, spread over `ctas`
+// CTAs by longest processing time first (a tile's cost is its problem's
+// number of candidate tiles), and the problems' 256-aligned row offsets.
+struct BatchedTcWork {
+    std::vector<int64_t> pad;     // B + 1 padded row offsets
+    std::vector<int64_t> begin;   // ctas + 1
+    std::vector<int4> items;
+    int ctas = 0;
+};
+
+static BatchedTcWork plan_batched_tc(const std::vector<int64_t> &off, int ctas_max) {
+    const size_t B = off.size() - 1;
+    BatchedTcWork w;
+    w.pad.resize(B + 1);
+    w.pad[0] = 0;
+    struct Tile {
+        int64_t cost;
+        int4 item;
+    };
+    std::vector<Tile> tiles;
+    for (size_t p = 0; p < B; ++p) {
+        const int64_t n = off[p + 1] - off[p];
+        w.pad[p + 1] = w.pad[p] + (n + 255) / 256 * 256;
+        const int64_t cost = (n + 127) / 128;
+        for (int64_t t = 0; t * 256 < n; ++t)
+            tiles.push_back({cost, make_int4((int)(w.pad[p] + 256 * t), (int)w.pad[p],
+                                             (int)(w.pad[p] + n), (int)(off[p] - w.pad[p]))});
+    }
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const Tile &a, const Tile &b) { return a.cost > b.cost; });
+    w.ctas = (int)std::min<int64_t>((int64_t)tiles.size(), ctas_max);
+    std::vector<std::vector<int4>> per(w.ctas);
+    std::vector<int64_t> load(w.ctas, 0);
+    for (const Tile &t : tiles) {
+        const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        per[c].push_back(t.item);
+        load[c] += t.cost;
+    }
+    w.begin.assign(w.ctas + 1, 0);
+    for (int c = 0; c < w.ctas; ++c) {
+        w.begin[c + 1] = w.begin[c] + (int64_t)per[c].size();
+        w.items.insert(w.items.end(), per[c].begin(), per[c].end());
+    }
+    return w;
+}
 
 struct ncvis_engine {
     ncvis_params p{};
@@ -379,8 +442,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     require(B < (size_t(1) << 20), "[ncvis] batched: too many problems");
     require(offsets[0] == 0, "[ncvis] batched: offsets[0] must be 0");
     int64_t min_n = INT64_MAX;
-    for (size_t p = 0; p < B; ++p) {
-        const int64_t n = offsets[p + 1] - offsets[p];
+    for (size_t q = 0; q < B; ++q) {
+        const int64_t n = offsets[q + 1] - offsets[q];
         require(n >= 2, "[ncvis] batched: every problem needs at least two points");
         min_n = std::min(min_n, n);
     }
@@ -389,7 +452,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     require(p.distance >= 0 && p.distance <= 3,
             "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
     require(p.d >= 1 && p.d <= 4, "[ncvis] batched: embedding dimension d must be in [1, 4]");
-    require(o.knn_precision == NCVIS_KNN_FP32, "[ncvis] batched: FP32 kNN only", kUnsupported);
+    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
     require(((uintptr_t)dY & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
     // k is clamped by the smallest problem (src/ncvis.cpp:381-382 per problem).
     int64_t kk = std::min<int64_t>((int64_t)p.n_neighbors, min_n - 1);
@@ -418,7 +481,15 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     while (h_tq[B] * kp.splits < 2 * num_sms() && kp.splits * 2 * kp.R <= 1024 &&
            min_n / (kp.splits * 2) >= 64)
         kp.splits *= 2;
-    const int C = kp.C();
+    KnnTcPlan tp = plan_knn_tc(total, (int)D, k, o.rerank_factor);
+    BatchedTcWork tw;
+    if (bf16) {
+        require(knn_tc_supported((int)D, tp.R),
+                "[ncvis] the BF16 tensor-core kNN supports D <= 128", kUnsupported);
+        tw = plan_batched_tc(h_off, num_sms());
+        require(tw.pad[B] < (int64_t(1) << 31), "[ncvis] batched: too many rows");
+    }
+    const int C = bf16 ? tp.R : kp.C();
     const int64_t max_chains = std::max<int64_t>(sgd_batched_resident_chains(d), (int64_t)B);
 
     Layout L;
@@ -445,6 +516,13 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     const size_t o_cq = L.take(sizeof(float) * max_chains);
     const size_t o_Yt = L.take(sizeof(float) * total * d);
     const size_t o_Qt = L.take(sizeof(float) * B);
+    const int64_t total_pad = bf16 ? tw.pad[B] : 0;
+    const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * total * tp.ldb) : 0;
+    const size_t o_Xbp = bf16 ? L.take(sizeof(__nv_bfloat16) * total_pad * tp.ldb) : 0;
+    const size_t o_sqp = bf16 ? L.take(sizeof(float) * total_pad) : 0;
+    const size_t o_pad = bf16 ? L.take(sizeof(int64_t) * (B + 1)) : 0;
+    const size_t o_wb = bf16 ? L.take(sizeof(int64_t) * (tw.ctas + 1)) : 0;
+    const size_t o_wi = bf16 ? L.take(sizeof(int4) * std::max<size_t>(tw.items.size(), 1)) : 0;
     char *base = ensure_arena(L.total);
     float *Xp = (float *)(base + o_Xp);
     float *sqn = (float *)(base + o_sqn);
@@ -472,7 +550,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     NCVIS_CUDA(cudaMemcpyAsync(d_seed, h_seed.data(), sizeof(uint64_t) * B, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
-    launch_preprocess(dX, total, (int)D, dist, Xp, sqn, nullptr, 0, flag, s);
+    __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
+    launch_preprocess(dX, total, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
     {
         int bad = 0;
@@ -481,12 +560,39 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
-    Segments seg;
-    seg.offsets = d_off;
-    seg.tile_prefix = d_tq;
-    seg.B = (int)B;
-    seg.n_tiles = h_tq[B];
-    launch_knn_select_f32(Xp, sqn, total, (int)D, dist, kp, cand_i, cand_d, s, seg);
+    if (bf16) {
+        // Problems at 256-aligned rows of a padded copy; one tensor-core launch
+        // over every problem's query tiles, each against its own rows.
+        __nv_bfloat16 *Xb_pad = (__nv_bfloat16 *)(base + o_Xbp);
+        float *sqn_pad = (float *)(base + o_sqp);
+        int64_t *d_pad = (int64_t *)(base + o_pad), *d_wb = (int64_t *)(base + o_wb);
+        int4 *d_wi = (int4 *)(base + o_wi);
+        NCVIS_CUDA(cudaMemcpyAsync(d_pad, tw.pad.data(), sizeof(int64_t) * (B + 1),
+                                   cudaMemcpyHostToDevice, s));
+        NCVIS_CUDA(cudaMemcpyAsync(d_wb, tw.begin.data(), sizeof(int64_t) * (tw.ctas + 1),
+                                   cudaMemcpyHostToDevice, s));
+        NCVIS_CUDA(cudaMemcpyAsync(d_wi, tw.items.data(), sizeof(int4) * tw.items.size(),
+                                   cudaMemcpyHostToDevice, s));
+        NCVIS_CUDA(cudaMemsetAsync(Xb_pad, 0, sizeof(__nv_bfloat16) * total_pad * tp.ldb, s));
+        NCVIS_CUDA(cudaMemsetAsync(sqn_pad, 0, sizeof(float) * total_pad, s));
+        NCVIS_LAUNCH(pad_rows, (unsigned)ceil_div(total * 32, 256), 256, 0, s, Xb, sqn, d_off,
+                     d_pad, (int)B, total, tp.ldb, Xb_pad, sqn_pad);
+        TcWork work{tw.ctas, d_wb, d_wi};
+        launch_knn_select_tc(Xb_pad, sqn_pad, total_pad, tp, dist, cand_i, cand_d, flag + 2, s,
+                             &work);
+        int timeout = 0;
+        NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NCVIS_CUDA(cudaStreamSynchronize(s));
+        require(timeout == 0, "[ncvis] kNN: the tensor-core kernel timed out waiting on a barrier",
+                kDeviceTimeout);
+    } else {
+        Segments seg;
+        seg.offsets = d_off;
+        seg.tile_prefix = d_tq;
+        seg.B = (int)B;
+        seg.n_tiles = h_tq[B];
+        launch_knn_select_f32(Xp, sqn, total, (int)D, dist, kp, cand_i, cand_d, s, seg);
+    }
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
     launch_rerank(Xp, total, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));

@@ -258,17 +258,53 @@ __device__ __forceinline__ void flush_queue(float (&ls)[R], int32_t (&li)[R], fl
     __syncwarp();
 }
 
+// One query tile of work: 256 rows from row0 (rows of the matrix the tensor
+// map covers), whose candidates are rows [lo, hi) of that matrix (lo a
+// multiple of 128); row r's candidate list goes to output row r + out_off and
+// its entries c are written as c + out_off.  Without a work list a CTA takes
+// the query tiles blockIdx.x, blockIdx.x + gridDim.x, ... of one problem of N
+// rows.
+struct QueryTile {
+    int64_t row0, lo, hi, out_off;
+};
+
+__device__ __forceinline__ int64_t work_items(const int64_t *__restrict__ work_begin,
+                                              int64_t n_qt) {
+    if (work_begin) return work_begin[blockIdx.x + 1] - work_begin[blockIdx.x];
+    return blockIdx.x < n_qt ? (n_qt - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+}
+
+__device__ __forceinline__ QueryTile work_item(const int64_t *__restrict__ work_begin,
+                                               const int4 *__restrict__ work, int64_t it,
+                                               int64_t N) {
+    QueryTile q;
+    if (work_begin) {
+        const int4 w = work[work_begin[blockIdx.x] + it];
+        q.row0 = w.x;
+        q.lo = w.y;
+        q.hi = w.z;
+        q.out_off = w.w;
+    } else {
+        q.row0 = ((int64_t)blockIdx.x + it * gridDim.x) * kQueryTile;
+        q.lo = 0;
+        q.hi = N;
+        q.out_off = 0;
+    }
+    return q;
+}
+
 template <int R, bool kIP>
 __global__ void __launch_bounds__(kThreads, 1)
     knn_select_tc(const __grid_constant__ CUtensorMap tmap, const float *__restrict__ sqnorm,
-                  int64_t N, int ksteps, int katoms, int32_t *__restrict__ cand_i,
+                  int64_t N, int ksteps, int katoms, const int64_t *__restrict__ work_begin,
+                  const int4 *__restrict__ work, int32_t *__restrict__ cand_i,
                   int *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     SharedStorage &s = *reinterpret_cast<SharedStorage *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
-    const int64_t n_ct = (N + kCandTile - 1) / kCandTile;
+    const int64_t n_items = work_items(work_begin, n_qt);
     const uint32_t a_bytes = 2u * katoms * kAtomBytes;
     const uint32_t b_bytes = (uint32_t)katoms * kAtomBytes;
 
@@ -308,17 +344,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int i = 0; i < kStages; ++i) issued[i] = false, issued_parity[i] = 0;
         bool a_issued = false;
         uint32_t a_parity = 0;
-        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
+        for (int64_t it = 0; it < n_items && !s.abort; ++it) {
+            const QueryTile q = work_item(work_begin, work, it, N);
             if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1)) break;
             mbar_expect_tx(&s.a_full, a_bytes);
             for (int h = 0; h < 2; ++h)
                 for (int at = 0; at < katoms; ++at)
-                    tma_load_2d(s.a[h][at], &tmap, &s.a_full, at * 64,
-                                (int)(qt * kQueryTile + h * 128));
+                    tma_load_2d(s.a[h][at], &tmap, &s.a_full, at * 64, (int)(q.row0 + h * 128));
             a_issued = true;
             a_parity = a_phase;
             a_phase ^= 1;
-            for (int64_t ct = 0; ct < n_ct; ++ct) {
+            for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2)) break;
                 mbar_expect_tx(&s.full[stage], b_bytes);
                 for (int at = 0; at < katoms; ++at)
@@ -343,11 +379,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         int stage = 0;
         uint32_t phase = 0, a_phase = 0, acc_phase = 0;
         int acc = 0;
-        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
+        for (int64_t it = 0; it < n_items && !s.abort; ++it) {
+            const QueryTile q = work_item(work_begin, work, it, N);
             if (!mbar_wait(s, &s.a_full, a_phase, err, 3)) break;
             a_phase ^= 1;
             tmem_fence_after();
-            for (int64_t ct = 0; ct < n_ct; ++ct) {
+            for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.acc_empty[acc], acc_phase ^ 1, err, 4)) break;
                 if (!mbar_wait(s, &s.full[stage], phase, err, 5)) break;
                 tmem_fence_after();
@@ -386,9 +423,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         constexpr int kC = (R <= 32 && kIP) ? 32 : 16;
         uint32_t acc_phase = 0;
         int acc = 0;
-        for (int64_t qt = blockIdx.x; qt < n_qt && !s.abort; qt += gridDim.x) {
-            const int64_t grow = qt * kQueryTile + row_in_tile;
-            const bool live = grow < N;
+        for (int64_t it = 0; it < n_items && !s.abort; ++it) {
+            const QueryTile q = work_item(work_begin, work, it, N);
+            const int64_t grow = q.row0 + row_in_tile;
+            const bool live = grow < q.hi;
             float ls[R];
             int32_t li[R];
 #pragma unroll
@@ -399,14 +437,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             float worst = FLT_MAX;
             int qlen = 0;
             bool ok = true;
-            for (int64_t ct = 0; ct < n_ct; ++ct) {
+            for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.acc_full[acc], acc_phase, err, 6)) {
                     ok = false;
                     break;
                 }
                 tmem_fence_after();
                 const int64_t c0 = ct * kCandTile;
-                const bool tail = c0 + kCandTile > N;
+                const bool tail = c0 + kCandTile > q.hi;
 #pragma unroll 1
                 for (int chunk = 0; chunk < kCandTile / kC; ++chunk) {
                     float v[kC];
@@ -421,14 +459,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                         for (int j = 0; j < kC; ++j) {
                             const int64_t c = cb + j;
-                            const float nc = (c < N) ? __ldg(sqnorm + c) : 0.f;
+                            const float nc = (c < q.hi) ? __ldg(sqnorm + c) : 0.f;
                             v[j] = fmaf(-2.f, v[j], nc);
                         }
                     }
                     if (tail) {
 #pragma unroll
                         for (int j = 0; j < kC; ++j)
-                            if (cb + j >= N) v[j] = kIP ? -FLT_MAX : FLT_MAX;
+                            if (cb + j >= q.hi) v[j] = kIP ? -FLT_MAX : FLT_MAX;
                     }
                     const float best = kIP ? -tree_reduce<true, kC>(v) : tree_reduce<false, kC>(v);
                     const bool hit = live && best < worst;
@@ -462,7 +500,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
             if (live) {
 #pragma unroll
-                for (int t = 0; t < R; ++t) cand_i[grow * R + t] = li[t];
+                for (int t = 0; t < R; ++t)
+                    cand_i[(grow + q.out_off) * R + t] =
+                        li[t] >= 0 ? (int32_t)(li[t] + q.out_off) : -1;
             }
         }
     }
@@ -507,7 +547,7 @@ bool knn_tc_supported(int D, int R) { return D >= 1 && D <= 64 * kMaxAtoms && (R
 
 void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
                           const KnnTcPlan &plan, int dist, int32_t *cand_i, float * /*cand_d*/,
-                          int *timeout_flag, cudaStream_t s) {
+                          int *timeout_flag, cudaStream_t s, const TcWork *work) {
     require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
     const int ksteps = (plan.ldb + 15) / 16;
     const int katoms = (ksteps * 16 + 63) / 64;
@@ -527,13 +567,16 @@ void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t 
             kCudaError);
     const size_t smem = sizeof(SharedStorage) + 1024;
     const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
-    const unsigned grid = (unsigned)std::min<int64_t>(n_qt, num_sms());
+    const unsigned grid =
+        work ? (unsigned)work->ctas : (unsigned)std::min<int64_t>(n_qt, num_sms());
     const bool ip = dist != kSquaredL2;
+    const int64_t *work_begin = work ? work->begin : nullptr;
+    const int4 *items = work ? work->items : nullptr;
     auto go = [&](auto kernel) {
         NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-        NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms, cand_i,
-                     timeout_flag);
+        NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms, work_begin,
+                     items, cand_i, timeout_flag);
     };
     if (plan.R == 32)
         ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);

@@ -53,9 +53,18 @@ struct KnnTcPlan {
 };
 KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor);
 bool knn_tc_supported(int D, int R);
+// Query tiles of several problems for one launch (device arrays): CTA b takes
+// items[begin[b] .. begin[b + 1]), each {row0, lo, hi, out_off} (int32): 256
+// query rows from row0, candidates rows [lo, hi) of Xb (lo a multiple of 256),
+// outputs at row + out_off with entries c + out_off.
+struct TcWork {
+    int ctas;
+    const int64_t *begin;
+    const int4 *items;
+};
 void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
                           const KnnTcPlan &plan, int dist, int32_t *cand_i, float *cand_d,
-                          int *timeout_flag, cudaStream_t s);
+                          int *timeout_flag, cudaStream_t s, const TcWork *work = nullptr);
 
 // ---- K5 symmetrize (src/knntable.cpp:24-99, src/ncvis.cpp:155-173) -----------
 size_t symmetrize_workspace_bytes(int64_t N, int k);

@@ -42,6 +42,27 @@ def test_batched_matches_single_problems(cuda, oracle):
         assert abs(tb - ts) <= 0.02, (len(X), tb, ts)
 
 
+def test_batched_bf16_knn_matches_single_problems(cuda):
+    """The tensor-core kNN over all problems in one launch (problems at
+    256-aligned rows of a padded copy, query tiles spread over the CTAs):
+    every problem's graph stays inside the problem, and its embedding quality
+    is within 0.02 of the single-problem path."""
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300 import quality
+    sizes = [300, 1000, 2600, 257, 4100, 900]
+    Xs = _problems(sizes, seed=9)
+    seeds = [21, 22, 23, 24, 25, 26]
+    vis = ncvis.NCVis(random_seed=3, knn_precision="bf16")
+    Ys = vis.fit_transform_batched(Xs, seeds=seeds)
+    assert [Y.shape for Y in Ys] == [(n, 2) for n in sizes]
+    for X, Y, sd in zip(Xs, Ys, seeds):
+        assert np.isfinite(Y).all()
+        Ysingle = ncvis.NCVis(random_seed=sd).fit_transform(X)
+        tb = quality.trustworthiness(X, Y, 15)
+        ts = quality.trustworthiness(X, Ysingle, 15)
+        assert abs(tb - ts) <= 0.02, (len(X), tb, ts)
+
+
 def test_batched_init_and_graph(cuda, oracle):
     """With no SGD epochs the batched output is each problem's init, which
     must match the oracle's one-thread init of that problem's graph."""
