@@ -3,22 +3,23 @@
 // in FP32 afterwards (K4, knn_simt.cu), which restores the reference's
 // distances (src/ncvis.cpp:72-153) on the selected set.
 //
-// Work decomposition (one persistent CTA per SM, 10 warps):
+// Work decomposition (one persistent CTA per SM, 11 warps):
 //   * a query tile is 256 preprocessed points (two M=128 halves), held in
 //     shared memory for the whole sweep (TMA, 128-byte swizzle, K-major);
-//   * candidate tiles of 128 points stream through a 4-stage TMA ring;
-//   * warp 0 issues TMA, warp 1 allocates TMEM and issues tcgen05.mma
-//     (M=128, N=128, K=16 steps) into one of two double-buffered 2x128-column
-//     FP32 accumulators (512 TMEM columns);
+//   * candidate tiles of 128 points stream through a 3-stage TMA ring;
+//   * warp 0 issues TMA; warps 1 and 10 issue tcgen05.mma (M=128, N=128,
+//     K=16 steps), one query half each, into one of two double-buffered
+//     2x128-column FP32 accumulators (512 TMEM columns; warp 1 allocates);
 //   * warps 2..9 own one query row each (TMEM lane = row; warp % 4 selects
-//     the lane quadrant): they read the accumulator with tcgen05.ld, turn dot
-//     products into ranking scores (-<q,c> for the inner-product spaces,
-//     |c|^2 - 2<q,c> for squared L2) and keep the R best candidates of their
-//     row sorted in registers.  A running worst-score threshold skips whole
-//     16-column chunks; in a chunk that holds candidates every lane compacts
-//     its qualifying ones into shared memory and the warp then feeds them, in
-//     lockstep, through a branchless insertion network (R compare-exchanges),
-//     so list updates cost no memory traffic and keep the warp converged.
+//     the lane quadrant): they read the accumulator with tcgen05.ld in
+//     32-column chunks, turn dot products into ranking scores (-<q,c> for the
+//     inner-product spaces, |c|^2 - 2<q,c> for squared L2), reduce each chunk
+//     with 3-input min/max trees and compare its best with the row's worst;
+//     qualifying candidates go to a per-row queue in shared memory, which the
+//     warp inserts into the rows' register-resident sorted lists in lockstep
+//     rounds (R compare-exchanges each) when a queue passes half full;
+//   * a CTA takes query tiles round-robin over one problem, or, for many
+//     problems in one launch, from a work list giving each tile its rows.
 // Every mbarrier wait is bounded in time: on expiry the CTA sets *err,
 // stops, drains its MMAs and in-flight TMA copies, frees TMEM and returns.
 #include <cuda.h>
@@ -40,9 +41,10 @@ constexpr int kCandTile = 128;    // candidates per tile (N=128)
 constexpr int kStages = 3;        // candidate-tile ring
 constexpr int kAtomBytes = 128 * 128;  // 128 rows x 128 bytes (64 bf16) per swizzle atom column
 constexpr int kMaxAtoms = 2;      // K <= 128
-constexpr int kThreads = 320;
+constexpr int kThreads = 352;
 constexpr int kEpiWarp0 = 2;
 constexpr int kEpiWarps = 8;
+constexpr int kMmaWarp1 = 10;  // issues the second query half's MMAs (warp 1 the first)
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kQueue = 32;  // per-row insertion queue slots (shared memory)
 constexpr uint32_t kTmemCols = 512;
@@ -309,17 +311,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t b_bytes = (uint32_t)katoms * kAtomBytes;
 
     if (threadIdx.x == 0) {
+        // Barriers the MMA issuers commit to take one arrival from each of the two.
         for (int i = 0; i < kStages; ++i) {
             mbar_init(&s.full[i], 1);
-            mbar_init(&s.empty[i], 1);
+            mbar_init(&s.empty[i], 2);
         }
         mbar_init(&s.a_full, 1);
-        mbar_init(&s.a_empty, 1);
+        mbar_init(&s.a_empty, 2);
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&s.acc_full[i], 1);
+            mbar_init(&s.acc_full[i], 2);
             mbar_init(&s.acc_empty[i], kEpiWarps);
         }
-        mbar_init(&s.drain, 1);
+        mbar_init(&s.drain, 2);
         s.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -374,8 +377,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (a_issued)
             while (!mbar_try_wait(&s.a_full, a_parity) && clock64() - t0 < kWaitCycles) {
             }
-    } else if (warp == 1 && lane == 0) {
-        // ---------------------------------------------------------- MMA issuer
+    } else if ((warp == 1 || warp == kMmaWarp1) && lane == 0) {
+        // ---------------------------------------------------------- MMA issuers
+        // Warp 1 issues query half 0's MMAs, warp kMmaWarp1 half 1's: two
+        // schedulers share the descriptor work of a tile.
+        const int h = (warp == 1) ? 0 : 1;
         int stage = 0;
         uint32_t phase = 0, a_phase = 0, acc_phase = 0;
         int acc = 0;
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!mbar_wait(s, &s.acc_empty[acc], acc_phase ^ 1, err, 4)) break;
                 if (!mbar_wait(s, &s.full[stage], phase, err, 5)) break;
                 tmem_fence_after();
-                for (int h = 0; h < 2; ++h) {
+                {
                     const uint32_t d_tmem = tmem + (uint32_t)(acc * 256 + h * 128);
                     for (int ks = 0; ks < ksteps; ++ks) {
                         const int at = ks >> 2;
@@ -411,7 +417,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const long long t0 = clock64();
         while (!mbar_try_wait(&s.drain, 0) && clock64() - t0 < kWaitCycles) {
         }
-    } else if (warp >= kEpiWarp0) {
+    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + kEpiWarps) {
         // ---------------------------------------------------------- epilogue
         const int h = (warp - kEpiWarp0) >> 2;
         const int quad = warp & 3;
