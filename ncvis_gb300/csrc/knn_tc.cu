@@ -474,23 +474,41 @@ __global__ void __launch_bounds__(kThreads, 1)
                         for (int j = 0; j < kC; ++j)
                             if (cb + j >= q.hi) v[j] = kIP ? -FLT_MAX : FLT_MAX;
                     }
-                    const float best = kIP ? -tree_reduce<true, kC>(v) : tree_reduce<false, kC>(v);
+                    // Best score of each 8-column group, then of the chunk.
+                    constexpr int kG = kC / 8;
+                    float gb[kG];
+#pragma unroll
+                    for (int g = 0; g < kG; ++g) {
+                        const float *w = v + 8 * g;
+                        gb[g] = kIP ? -max3f(max3f(w[0], w[1], w[2]), max3f(w[3], w[4], w[5]),
+                                             fmaxf(w[6], w[7]))
+                                    : min3f(min3f(w[0], w[1], w[2]), min3f(w[3], w[4], w[5]),
+                                            fminf(w[6], w[7]));
+                    }
+                    const float best = tree_reduce<false, kG>(gb);
                     const bool hit = live && best < worst;
                     if (!__any_sync(0xffffffffu, hit)) continue;
-                    // Qualifying candidates are queued (16 columns at a time);
-                    // a queue past half full is flushed into the lists first.
+                    // Qualifying candidates are queued 16 columns at a time,
+                    // looking only into the 8-column groups whose best beats
+                    // the row's worst; a queue past half full is flushed into
+                    // the lists first.
 #pragma unroll
                     for (int half = 0; half < kC / 16; ++half) {
                         if (__any_sync(0xffffffffu, qlen > kQueue - 16))
                             flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
                         if (hit) {
 #pragma unroll
-                            for (int j = 0; j < 16; ++j) {
-                                const float x = kIP ? -v[half * 16 + j] : v[half * 16 + j];
-                                if (x < worst) {
-                                    s.queue_v[qlen][etid] = x;
-                                    s.queue_i[qlen][etid] = (int32_t)(cb + half * 16 + j);
-                                    ++qlen;
+                            for (int g = 2 * half; g < 2 * half + 2; ++g) {
+                                if (gb[g] < worst) {
+#pragma unroll
+                                    for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                                        const float x = kIP ? -v[j] : v[j];
+                                        if (x < worst) {
+                                            s.queue_v[qlen][etid] = x;
+                                            s.queue_i[qlen][etid] = (int32_t)(cb + j);
+                                            ++qlen;
+                                        }
+                                    }
                                 }
                             }
                         }
