@@ -423,10 +423,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int quad = warp & 3;
         const int etid = threadIdx.x - kEpiWarp0 * 32;
         const int row_in_tile = h * 128 + quad * 32 + lane;
-        // Accumulator columns per tcgen05.ld: 32 for 32-entry lists and the
-        // inner-product scan; 16 where 64-entry lists or the squared-L2 norm
-        // terms leave fewer registers.
-        constexpr int kC = (R <= 32 && kIP) ? 32 : 16;
+        // Accumulator columns per tcgen05.ld: 32 with 32-entry lists; 64-entry
+        // lists leave registers for 16.
+        constexpr int kC = R <= 32 ? 32 : 16;
         uint32_t acc_phase = 0;
         int acc = 0;
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
@@ -462,11 +461,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                     // Scores, lower is better: |c|^2 - 2<q,c> (squared L2) or
                     // -<q,c> (kept as +<q,c>, compared against -worst).
                     if constexpr (!kIP) {
+                        // The chunk's candidate norms, the same for every lane:
+                        // 16-byte loads where the chunk lies inside the rows.
+                        if (cb + kC <= q.hi) {
 #pragma unroll
-                        for (int j = 0; j < kC; ++j) {
-                            const int64_t c = cb + j;
-                            const float nc = (c < q.hi) ? __ldg(sqnorm + c) : 0.f;
-                            v[j] = fmaf(-2.f, v[j], nc);
+                            for (int j = 0; j < kC; j += 4) {
+                                const float4 nc =
+                                    __ldg(reinterpret_cast<const float4 *>(sqnorm + cb + j));
+                                v[j] = fmaf(-2.f, v[j], nc.x);
+                                v[j + 1] = fmaf(-2.f, v[j + 1], nc.y);
+                                v[j + 2] = fmaf(-2.f, v[j + 2], nc.z);
+                                v[j + 3] = fmaf(-2.f, v[j + 3], nc.w);
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < kC; ++j) {
+                                const int64_t c = cb + j;
+                                const float nc = (c < q.hi) ? __ldg(sqnorm + c) : 0.f;
+                                v[j] = fmaf(-2.f, v[j], nc);
+                            }
                         }
                     }
                     if (tail) {
@@ -519,6 +532,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (lane == 0) mbar_arrive(&s.acc_empty[acc]);
                 acc ^= 1;
                 if (acc == 0) acc_phase ^= 1;
+                // Queues past half full are flushed here, after the accumulator
+                // is released, so that the MMAs of the next tiles go on meanwhile;
+                // a flush inside the tile happens only when one tile overfills a
+                // queue (early in the sweep).
+                if (__any_sync(0xffffffffu, qlen > kQueue - 16))
+                    flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
             }
             if (!ok) break;
             flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
@@ -577,6 +596,7 @@ void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t 
     const int katoms = (ksteps * 16 + 63) / 64;
     require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
     require(((uintptr_t)Xb & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
+    require(((uintptr_t)sqnorm & 15) == 0, "knn: squared norms must be 16-byte aligned");
     CUtensorMap map;
     cuuint64_t dims[2] = {(cuuint64_t)plan.ldb, (cuuint64_t)N};
     cuuint64_t strides[1] = {(cuuint64_t)plan.ldb * 2};

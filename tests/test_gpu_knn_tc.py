@@ -1,8 +1,9 @@
 """K2 BF16 tensor-core kNN (tcgen05, TMA, TMEM) + K4 exact FP32 rerank.
 
 The candidate selection runs on BF16 copies of the preprocessed points with
-FP32 accumulation, keeps 4k candidates per point, and the rerank restores the
-exact FP32 distances and the reference's row contract.  Bar: recall@15
+FP32 accumulation, keeps 32 candidates per point (2k for k = 15, the default)
+or 64 (rerank_factor 4: the 4k = 60 the headline configuration names), and the
+rerank restores the exact FP32 distances and the reference's row contract.  Bar: recall@15
 against FP64 exact search >= 0.99 (the 131,072 x 100 vMF configuration is
 checked on a 2000-query subsample), every returned distance equal to the
 FP32 distance of its pair to 1e-5 relative, rows in descending order."""
@@ -14,9 +15,10 @@ from conftest import gmm
 pytestmark = pytest.mark.gpu
 
 
-def _knn(cuda, X, k, dist, precision=1):
+def _knn(cuda, X, k, dist, precision=1, rerank_factor=0):
     from ncvis_gb300 import stages
-    inds, dists = stages.knn(cuda.tensor(X, device="cuda"), k, dist, precision=precision)
+    inds, dists = stages.knn(cuda.tensor(X, device="cuda"), k, dist, precision=precision,
+                             rerank_factor=rerank_factor)
     return inds.cpu().numpy().astype(np.int64), dists.cpu().numpy()
 
 
@@ -57,6 +59,19 @@ def test_vmf_131072_recall(cuda, oracle):
     assert gi.min() >= 0 and gi.max() < 131072
 
 
+def test_vmf_131072_recall_64_candidates(cuda, oracle):
+    from ncvis_gb300.synthetic import vmf_mixture
+    X, _ = vmf_mixture(131072, 100, n_comp=32, kappa=50.0, seed=7)
+    gi, gd = _knn(cuda, X, 15, 2, rerank_factor=4)
+    rng = np.random.default_rng(1)
+    q = np.sort(rng.choice(131072, 1000, replace=False))
+    exact = _fp64_rows(oracle.preprocess(X, 2), q, 15, 2)
+    r = _recall(gi[q], exact)
+    print(f"recall@15 (64 candidates): {r:.5f}")
+    assert r >= 0.99
+    assert np.all(np.diff(gd, axis=1) <= 0)
+
+
 @pytest.mark.parametrize("dist", [0, 1, 2, 3])
 def test_distances_small(cuda, oracle, dist):
     X, _ = gmm(3000, 24, 6, 3.0, seed=10 + dist)
@@ -72,12 +87,13 @@ def test_distances_small(cuda, oracle, dist):
             assert abs(gd[i, j] - ref) <= 1e-5 * max(1.0, abs(ref))
 
 
+@pytest.mark.parametrize("rf", [2, 4])
 @pytest.mark.parametrize("N,D", [(17, 3), (200, 1), (255, 16), (257, 100), (1000, 128), (4097, 64)])
-def test_shapes_and_tails(cuda, oracle, N, D):
+def test_shapes_and_tails(cuda, oracle, N, D, rf):
     rng = np.random.default_rng(N + D)
     X = rng.normal(size=(N, D)).astype(np.float32)
     k = min(15, N - 1)
-    gi, gd = _knn(cuda, X, k, 0)
+    gi, gd = _knn(cuda, X, k, 0, rerank_factor=rf)
     oi, _ = oracle.knn(oracle.preprocess(X, 0), 0, k, use_f64=True)
     assert gi.min() >= 0 and gi.max() < N
     if D >= 3:
