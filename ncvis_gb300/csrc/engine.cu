@@ -295,10 +295,11 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
 
     cudaStream_t s = stream();
     KnnPlan kp = plan_knn_f32((int64_t)N, k, o.rerank_factor);
-    KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, k, o.rerank_factor);
+    KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, k, o.rerank_factor, dist);
     if (bf16)
         require(knn_tc_supported((int)D, tp.R),
                 "[ncvis] the BF16 tensor-core kNN supports D <= 128", kUnsupported);
+    const bool fold = bf16 && tp.fold;
     const int C = bf16 ? tp.R : kp.C();
     const int64_t nk = (int64_t)N * k;
     const int chains = o.sgd_chains > 0 ? o.sgd_chains : 0;  // 0: sized once E is known
@@ -310,6 +311,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const size_t o_sqn = L.take(sizeof(float) * N);
     const size_t o_flag = L.take(sizeof(int) * 4);
     const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
+    const size_t o_Xc = fold ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
     const size_t o_ci = L.take(sizeof(int32_t) * N * C);
     const size_t o_cd = L.take(sizeof(float) * N * C);
     const size_t o_ki = L.take(sizeof(int32_t) * nk);
@@ -331,6 +333,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     float *sqn = (float *)(base + o_sqn);
     int *flag = (int *)(base + o_flag);
     __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
+    __nv_bfloat16 *Xc = fold ? (__nv_bfloat16 *)(base + o_Xc) : nullptr;
     int32_t *cand_i = (int32_t *)(base + o_ci);
     float *cand_d = (float *)(base + o_cd);
     int32_t *knn_i = (int32_t *)(base + o_ki);
@@ -347,7 +350,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         NCVIS_CUDA(cudaMemcpyAsync((void *)dX, X, sizeof(float) * N * D, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
-    launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s);
+    launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s, Xc);
     NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
     {
         int bad = 0;
@@ -357,7 +360,8 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     }
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
     if (bf16)
-        launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s);
+        launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s, nullptr,
+                             Xc);
     else
         launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
@@ -481,7 +485,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     while (h_tq[B] * kp.splits < 2 * num_sms() && kp.splits * 2 * kp.R <= 1024 &&
            min_n / (kp.splits * 2) >= 64)
         kp.splits *= 2;
-    KnnTcPlan tp = plan_knn_tc(total, (int)D, k, o.rerank_factor);
+    KnnTcPlan tp = plan_knn_tc(total, (int)D, k, o.rerank_factor, dist);
+    const bool fold = bf16 && tp.fold;
     BatchedTcWork tw;
     if (bf16) {
         require(knn_tc_supported((int)D, tp.R),
@@ -519,6 +524,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     const int64_t total_pad = bf16 ? tw.pad[B] : 0;
     const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * total * tp.ldb) : 0;
     const size_t o_Xbp = bf16 ? L.take(sizeof(__nv_bfloat16) * total_pad * tp.ldb) : 0;
+    const size_t o_Xc = fold ? L.take(sizeof(__nv_bfloat16) * total * tp.ldb) : 0;
+    const size_t o_Xcp = fold ? L.take(sizeof(__nv_bfloat16) * total_pad * tp.ldb) : 0;
     const size_t o_sqp = bf16 ? L.take(sizeof(float) * total_pad) : 0;
     const size_t o_pad = bf16 ? L.take(sizeof(int64_t) * (B + 1)) : 0;
     const size_t o_wb = bf16 ? L.take(sizeof(int64_t) * (tw.ctas + 1)) : 0;
@@ -551,7 +558,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
     __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
-    launch_preprocess(dX, total, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s);
+    __nv_bfloat16 *Xc = fold ? (__nv_bfloat16 *)(base + o_Xc) : nullptr;
+    launch_preprocess(dX, total, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s, Xc);
     NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
     {
         int bad = 0;
@@ -577,9 +585,16 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         NCVIS_CUDA(cudaMemsetAsync(sqn_pad, 0, sizeof(float) * total_pad, s));
         NCVIS_LAUNCH(pad_rows, (unsigned)ceil_div(total * 32, 256), 256, 0, s, Xb, sqn, d_off,
                      d_pad, (int)B, total, tp.ldb, Xb_pad, sqn_pad);
+        __nv_bfloat16 *Xc_pad = nullptr;
+        if (fold) {
+            Xc_pad = (__nv_bfloat16 *)(base + o_Xcp);
+            NCVIS_CUDA(cudaMemsetAsync(Xc_pad, 0, sizeof(__nv_bfloat16) * total_pad * tp.ldb, s));
+            NCVIS_LAUNCH(pad_rows, (unsigned)ceil_div(total * 32, 256), 256, 0, s, Xc, sqn, d_off,
+                         d_pad, (int)B, total, tp.ldb, Xc_pad, sqn_pad);
+        }
         TcWork work{tw.ctas, d_wb, d_wi};
         launch_knn_select_tc(Xb_pad, sqn_pad, total_pad, tp, dist, cand_i, cand_d, flag + 2, s,
-                             &work);
+                             &work, Xc_pad);
         int timeout = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
@@ -786,7 +801,8 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
         const bool bf16 = (precision == NCVIS_KNN_BF16_RERANK);
         cudaStream_t s = (cudaStream_t)stream;
         KnnPlan kp = plan_knn_f32((int64_t)N, (int)k, rerank_factor);
-        KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, (int)k, rerank_factor);
+        KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, (int)k, rerank_factor, distance);
+        const bool fold = bf16 && tp.fold;
         if (bf16)
             require(knn_tc_supported((int)D, tp.R),
                     "knn: the BF16 tensor-core kNN supports D <= 128", kUnsupported);
@@ -798,13 +814,15 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
         const size_t o_ci = L.take(sizeof(int32_t) * N * C);
         const size_t o_cd = L.take(sizeof(float) * N * C);
         const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
+        const size_t o_Xc = fold ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
         char *base = nullptr;
         NCVIS_CUDA(cudaMallocAsync((void **)&base, L.total, s));
         NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int) * 2, s));
         __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
+        __nv_bfloat16 *Xc = fold ? (__nv_bfloat16 *)(base + o_Xc) : nullptr;
         launch_preprocess(dX, (int64_t)N, (int)D, distance, (float *)(base + o_Xp),
                           (float *)(base + o_sqn), Xb, bf16 ? tp.ldb : 0, (int *)(base + o_flag),
-                          s);
+                          s, Xc);
         int bad = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&bad, base + o_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
@@ -816,7 +834,7 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
         if (bf16) {
             launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
                                  (int32_t *)(base + o_ci), (float *)(base + o_cd),
-                                 (int *)(base + o_flag) + 1, s);
+                                 (int *)(base + o_flag) + 1, s, nullptr, Xc);
             int timeout = 0;
             NCVIS_CUDA(cudaMemcpyAsync(&timeout, (int *)(base + o_flag) + 1, sizeof(int),
                                        cudaMemcpyDeviceToHost, s));

@@ -19,7 +19,12 @@
 //     warp inserts into the rows' register-resident sorted lists in lockstep
 //     rounds (R compare-exchanges each) when a queue passes half full;
 //   * a CTA takes query tiles round-robin over one problem, or, for many
-//     problems in one launch, from a work list giving each tile its rows.
+//     problems in one launch, from a work list giving each tile its rows;
+//   * squared L2 with D <= 126 folds the candidate norms into the product:
+//     candidates come from a second BF16 copy whose columns D, D + 1 hold
+//     -|c|^2 / 2 as a BF16 high and low part, the queries' copy 1, 1 there, so
+//     the accumulator holds <q, c> - |c|^2 / 2 and the scan is the
+//     inner-product one (otherwise the scan adds the FP32 norms per column).
 // Every mbarrier wait is bounded in time: on expiry the CTA sets *err,
 // stops, drains its MMAs and in-flight TMA copies, frees TMEM and returns.
 #include <cuda.h>
@@ -297,7 +302,8 @@ __device__ __forceinline__ QueryTile work_item(const int64_t *__restrict__ work_
 
 template <int R, bool kIP>
 __global__ void __launch_bounds__(kThreads, 1)
-    knn_select_tc(const __grid_constant__ CUtensorMap tmap, const float *__restrict__ sqnorm,
+    knn_select_tc(const __grid_constant__ CUtensorMap tmap,
+                  const __grid_constant__ CUtensorMap tmap_c, const float *__restrict__ sqnorm,
                   int64_t N, int ksteps, int katoms, const int64_t *__restrict__ work_begin,
                   const int4 *__restrict__ work, int32_t *__restrict__ cand_i,
                   int *__restrict__ err) {
@@ -361,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2)) break;
                 mbar_expect_tx(&s.full[stage], b_bytes);
                 for (int at = 0; at < katoms; ++at)
-                    tma_load_2d(s.b[stage][at], &tmap, &s.full[stage], at * 64,
+                    tma_load_2d(s.b[stage][at], &tmap_c, &s.full[stage], at * 64,
                                 (int)(ct * kCandTile));
                 issued[stage] = true;
                 issued_parity[stage] = phase;
@@ -573,14 +579,16 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 }  // namespace
 
-KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor) {
+KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor, int dist) {
     KnnTcPlan p;
     // Default: 2k candidates (32 for k = 15), which measured recall@15 = 1.0
     // against FP64 search at 1,024,000 x 100; rerank_factor = 4 keeps 64.
     if (rerank_factor <= 0) rerank_factor = 2;
     const int64_t want = std::max<int64_t>((int64_t)rerank_factor * k, (int64_t)k + 1);
     p.R = want <= 32 ? 32 : 64;  // the kernel keeps 32 or 64 candidates per point
-    p.ldb = (D + 7) / 8 * 8;
+    // Squared L2 folds -|c|^2 / 2 into two extra K columns when they fit (D <= 126).
+    p.fold = (dist == kSquaredL2) && D + 2 <= 64 * kMaxAtoms;
+    p.ldb = (D + (p.fold ? 2 : 0) + 7) / 8 * 8;
     p.Npad = N;
     (void)N;
     return p;
@@ -588,39 +596,49 @@ KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor) {
 
 bool knn_tc_supported(int D, int R) { return D >= 1 && D <= 64 * kMaxAtoms && (R == 32 || R == 64); }
 
+
 void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
                           const KnnTcPlan &plan, int dist, int32_t *cand_i, float * /*cand_d*/,
-                          int *timeout_flag, cudaStream_t s, const TcWork *work) {
+                          int *timeout_flag, cudaStream_t s, const TcWork *work,
+                          const __nv_bfloat16 *Xc) {
     require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
     const int ksteps = (plan.ldb + 15) / 16;
     const int katoms = (ksteps * 16 + 63) / 64;
     require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
     require(((uintptr_t)Xb & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
     require(((uintptr_t)sqnorm & 15) == 0, "knn: squared norms must be 16-byte aligned");
-    CUtensorMap map;
-    cuuint64_t dims[2] = {(cuuint64_t)plan.ldb, (cuuint64_t)N};
-    cuuint64_t strides[1] = {(cuuint64_t)plan.ldb * 2};
-    cuuint32_t box[2] = {64, 128};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)Xb, dims,
-                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_128B,
-                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    require(r == CUDA_SUCCESS, "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")",
-            kCudaError);
+    require(!plan.fold || (Xc && ((uintptr_t)Xc & 15) == 0),
+            "knn: the folded squared-L2 mode needs a 16-byte aligned candidate copy");
+    auto encode = [&](const __nv_bfloat16 *base, CUtensorMap &map) {
+        cuuint64_t dims[2] = {(cuuint64_t)plan.ldb, (cuuint64_t)N};
+        cuuint64_t strides[1] = {(cuuint64_t)plan.ldb * 2};
+        cuuint32_t box[2] = {64, 128};
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base,
+                                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                          CU_TENSOR_MAP_SWIZZLE_128B,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        require(r == CUDA_SUCCESS,
+                "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")", kCudaError);
+    };
+    // Queries come from Xb, candidates from Xc in the folded mode (else Xb).
+    CUtensorMap map, map_c;
+    encode(Xb, map);
+    encode(plan.fold ? Xc : Xb, map_c);
     const size_t smem = sizeof(SharedStorage) + 1024;
     const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
     const unsigned grid =
         work ? (unsigned)work->ctas : (unsigned)std::min<int64_t>(n_qt, num_sms());
-    const bool ip = dist != kSquaredL2;
+    // The folded squared-L2 product <q, c> - |c|^2 / 2 ranks like an inner product.
+    const bool ip = dist != kSquaredL2 || plan.fold;
     const int64_t *work_begin = work ? work->begin : nullptr;
     const int4 *items = work ? work->items : nullptr;
     auto go = [&](auto kernel) {
         NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-        NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, sqnorm, N, ksteps, katoms, work_begin,
-                     items, cand_i, timeout_flag);
+        NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, map_c, sqnorm, N, ksteps, katoms,
+                     work_begin, items, cand_i, timeout_flag);
     };
     if (plan.R == 32)
         ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);

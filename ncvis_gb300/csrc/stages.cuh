@@ -16,8 +16,11 @@ enum Distance { kSquaredL2 = 0, kInnerProduct = 1, kCosine = 2, kCorrelation = 3
 // Xp[N, D] f32 preprocessed rows, sqnorm[N] = |xp|^2, and (if Xb != nullptr)
 // Xb[N, ldb] bf16 copies zero-padded to ldb columns.  bad_flag (device int)
 // is set to 1 if any input is not finite.
+// Xc (optional, squared L2 on the tensor cores): candidate copy whose columns
+// D, D + 1 hold -|x|^2 / 2 as BF16 high + low parts; Xb then holds 1, 1 there.
 void launch_preprocess(const float *X, int64_t N, int D, int dist, float *Xp, float *sqnorm,
-                       __nv_bfloat16 *Xb, int ldb, int *bad_flag, cudaStream_t s);
+                       __nv_bfloat16 *Xb, int ldb, int *bad_flag, cudaStream_t s,
+                       __nv_bfloat16 *Xc = nullptr);
 
 // Independent problems packed in one point array: problem p owns rows
 // [offsets[p], offsets[p+1]) (device arrays).  B == 0: one problem, all rows.
@@ -49,9 +52,10 @@ void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *c
 struct KnnTcPlan {
     int R;       // candidates kept per point (multiple of 4 is not required)
     int ldb;     // padded row length of Xb (bf16 elements)
+    bool fold;   // squared L2 with the norms folded into the product (needs Xc)
     int64_t Npad;
 };
-KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor);
+KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor, int dist);
 bool knn_tc_supported(int D, int R);
 // Query tiles of several problems for one launch (device arrays): CTA b takes
 // items[begin[b] .. begin[b + 1]), each {row0, lo, hi, out_off} (int32): 256
@@ -64,7 +68,8 @@ struct TcWork {
 };
 void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
                           const KnnTcPlan &plan, int dist, int32_t *cand_i, float *cand_d,
-                          int *timeout_flag, cudaStream_t s, const TcWork *work = nullptr);
+                          int *timeout_flag, cudaStream_t s, const TcWork *work = nullptr,
+                          const __nv_bfloat16 *Xc = nullptr);
 
 // ---- K5 symmetrize (src/knntable.cpp:24-99, src/ncvis.cpp:155-173) -----------
 size_t symmetrize_workspace_bytes(int64_t N, int k);
