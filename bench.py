@@ -253,6 +253,48 @@ def update_ceiling(rows, rate):
             "frac_of_update_ceiling": rate / u.value}
 
 
+def small_config(dev):
+    """The reference's own CPU-runnable case, whole fit_transform on both sides:
+    10,000 x 64 float32 points of a 10-component Gaussian mixture (centres
+    ~ N(0, 25 I), sigma 1, equal weights, seed 42) at the reference's defaults
+    (squared L2, k=15, d=2, 50 epochs, 20 init epochs, default noise plan and
+    a/b).  GPU: the plain FP32 path (the drop-in), median of 5 device-timed
+    fits.  CPU: the oracle (the reference's algorithm restated; brute-force
+    kNN where the reference uses HNSW) on all host threads, median of 3."""
+    import torch
+    import ncvis_gb300 as ncvis
+    from ncvis_gb300.api import default_noise_plan, find_ab_params
+    from ncvis_gb300.synthetic import gaussian_mixture
+    from oracle import oracle as O
+    X, _ = gaussian_mixture(10_000, 64, 10, 5.0, 1.0, seed=42)
+    Xd = torch.from_numpy(X).to(dev)
+    vis = ncvis.NCVis(random_seed=42)
+    for _ in range(2):
+        vis.fit_transform(Xd)
+    gpu = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        vis.fit_transform(Xd)
+        b.record()
+        torch.cuda.synchronize()
+        gpu.append(a.elapsed_time(b) / 1000.0)
+    av, bv = find_ab_params(1.0, 0.4)
+    plan = default_noise_plan(EPOCHS).astype(np.uint64)
+    threads = os.cpu_count() or 1
+    cpu = []
+    for _ in range(3):
+        t = time.perf_counter()
+        O.fit_transform(X, 2, K_NN, 42, EPOCHS, INIT_EPOCHS, av, bv, 1.0, 1.0, plan, 0, threads)
+        cpu.append(time.perf_counter() - t)
+    g, c = statistics.median(gpu), statistics.median(cpu)
+    return {"workload": "fit_transform 10,000 x 64 Gaussian mixture, reference defaults "
+                        "(squared L2, k=15, d=2, 50 epochs)",
+            "gpu_plain_fp32_s": g, "cpu_reference_algorithm_s": c, "cpu_threads": threads,
+            "cpu_knn": "brute force (the reference's HNSW is unavailable)",
+            "speedup": c / g}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -385,9 +427,11 @@ def run_ours(args):
         }
 
     cpu = None
+    small = None
     if not args.no_cpu_baseline and world == 1:
         cpu_full = cpu_sample_pipeline(os.cpu_count() or 1, 1, 0, log=lambda m: print(m, file=sys.stderr))
         cpu = {k: cpu_full[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        small = small_config(dev)
 
     line = {
         "metric": "fit_transform_seconds", "value": step_s, "unit": "s", "n_gpus": world,
@@ -409,6 +453,7 @@ def run_ours(args):
                      ("preprocess_ms", "knn_ms", "rerank_ms", "symmetrize_ms", "init_ms",
                       "optimize_ms")},
         "cpu_baseline": cpu,
+        "small_config": small,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }

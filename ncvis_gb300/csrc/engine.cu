@@ -146,6 +146,21 @@ __global__ void pad_rows(const __nv_bfloat16 *__restrict__ Xb, const float *__re
 
 using namespace ncvis_gpu;
 
+// Whether the current device reads pageable host memory coherently
+// (cudaDevAttrPageableMemoryAccess), cached per device.
+static bool reads_pageable_host_memory() {
+    static std::mutex mu;
+    static std::map<int, bool> known;
+    int dev = 0;
+    NCVIS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = known.find(dev);
+    if (it != known.end()) return it->second;
+    int v = 0;
+    NCVIS_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev));
+    return known[dev] = (v != 0);
+}
+
 // Query tiles of the problems for one tensor-core launch, spread over `ctas`
 // CTAs by longest processing time first (a tile's cost is its problem's
 // number of candidate tiles), and the problems' 256-aligned row offsets.
@@ -305,7 +320,11 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const int chains = o.sgd_chains > 0 ? o.sgd_chains : 0;  // 0: sized once E is known
 
     Layout L;
-    const size_t o_X = host ? L.take(sizeof(float) * N * D) : 0;
+    // Host X is read in place by the preprocessing kernel where the device
+    // reads pageable host memory coherently (e.g. through the host's page
+    // tables); elsewhere it is first copied to the device.
+    const bool read_host = host && reads_pageable_host_memory();
+    const size_t o_X = (host && !read_host) ? L.take(sizeof(float) * N * D) : 0;
     const size_t o_Y = host ? L.take(sizeof(float) * N * d) : 0;
     const size_t o_Xp = L.take(sizeof(float) * N * D);
     const size_t o_sqn = L.take(sizeof(float) * N);
@@ -327,7 +346,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const size_t o_stream = replay ? L.take(sizeof(int32_t) * std::max<size_t>(o.replay_len, 1)) : 0;
     char *base = ensure_arena(L.total);
 
-    const float *dX = host ? (float *)(base + o_X) : X;
+    const float *dX = (host && !read_host) ? (float *)(base + o_X) : X;
     float *dY = host ? (float *)(base + o_Y) : Y;
     float *Xp = (float *)(base + o_Xp);
     float *sqn = (float *)(base + o_sqn);
@@ -346,7 +365,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
 
     Events ev;
     NCVIS_CUDA(cudaEventRecord(ev.ev[0], s));
-    if (host)
+    if (host && !read_host)
         NCVIS_CUDA(cudaMemcpyAsync((void *)dX, X, sizeof(float) * N * D, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
