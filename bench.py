@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--knn", choices=["fp32", "bf16"], default="bf16")
+    p.add_argument("--sgd", choices=["hogwild", "hogwild_unstaged"], default="hogwild",
+                   help="optimizer noise: staged in shared-memory windows (default) or read "
+                        "from the whole embedding")
     p.add_argument("--n", type=int, default=N_FULL, help="points (default: the full workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-recall", action="store_true")
@@ -238,19 +241,23 @@ def recall_at_15(X, inds, n_queries=2000, seed=0):
     return hits / (n_queries * K_NN)
 
 
-def update_ceiling(rows, rate):
+def update_ceiling(rows, rate, positive_pairs, opt_ms):
     """The GPU's rate for the optimizer's per-sample traffic (a random row
     gather plus a random row reduction over an L2-resident array of `rows`
-    2-float rows), measured live, and the SGD's pair-update rate as a
-    fraction of it."""
+    2-float rows), measured live; the SGD's pair-update rate as a fraction of
+    it; and the floor it sets for the positive samples alone (every positive
+    sample is such a random gather + reduction; staged noise samples are
+    served from shared memory)."""
     import ctypes as C
     from ncvis_gb300 import _lib
     g, u = C.c_double(0), C.c_double(0)
     rc = _lib.lib().ncvis_measure_update_rate(rows, D_EMB, C.byref(g), C.byref(u), None)
     if rc != 0:
         return {"update_ceiling_error": _lib.lib().ncvis_get_last_error().decode()}
+    floor_ms = positive_pairs / u.value * 1e3
     return {"gather_ceiling_per_s": g.value, "update_ceiling_per_s": u.value,
-            "frac_of_update_ceiling": rate / u.value}
+            "frac_of_update_ceiling": rate / u.value, "positive_floor_ms": floor_ms,
+            "frac_of_positive_floor": floor_ms / opt_ms}
 
 
 def small_config(dev):
@@ -310,7 +317,8 @@ def run_ours(args):
     X = workload(n)
     Xd = torch.from_numpy(X).to(dev)
     vis = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
-                      random_seed=42, distance="cosine", knn_precision=args.knn)
+                      random_seed=42, distance="cosine", knn_precision=args.knn,
+                      sgd_mode=args.sgd)
     for _ in range(args.warmup):
         vis.fit_transform(Xd)
     torch.cuda.synchronize()
@@ -396,7 +404,8 @@ def run_ours(args):
         from ncvis_gb300 import quality as Qm
         Y_ours = vis.fit_transform(Xd)
         plain = ncvis.NCVis(d=D_EMB, n_neighbors=K_NN, n_epochs=EPOCHS, n_init_epochs=INIT_EPOCHS,
-                            random_seed=42, distance="cosine", knn_precision="fp32")
+                            random_seed=42, distance="cosine", knn_precision="fp32",
+                            sgd_mode="hogwild_unstaged")
         plain.fit_transform(Xd)  # warm-up (arena, kernels)
         torch.cuda.synchronize()
         t_plain = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -445,7 +454,9 @@ def run_ours(args):
         "sgd": {"pair_updates_per_s": pair_updates / (opt_ms / 1000.0),
                 "edge_epochs_per_s": E * EPOCHS / (opt_ms / 1000.0), "optimize_ms": opt_ms,
                 "algorithmic_GBps": sgd_gbs, "hbm_peak_GBps": hbm, "frac_of_hbm": sgd_gbs / hbm,
-                **update_ceiling(n, pair_updates / (opt_ms / 1000.0)),
+                **update_ceiling(n, pair_updates / (opt_ms / 1000.0), E * EPOCHS, opt_ms),
+                "noise": ("staged in shared-memory windows" if args.sgd == "hogwild"
+                          else "each sample read from the whole embedding"),
                 "E": E},
         "recall_at_15": recall,
         "quality": quality,

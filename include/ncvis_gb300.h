@@ -16,6 +16,7 @@
  *                                   src/knntable.cpp:24-99, src/ncvis.cpp:155-173
  *   ncvis_init_embedding_device  <- NCVis::init_embedding       src/ncvis.cpp:184-273
  *   ncvis_optimize_device        <- NCVis::optimize             src/ncvis.cpp:275-352
+ *   ncvis_optimize_staged_device <- NCVis::optimize, noise staged src/ncvis.cpp:275-352
  *   ncvis_optimize_replay_device <- NCVis::optimize, one thread src/ncvis.cpp:275-352
  * The C++ header include/ncvis.hpp wraps this ABI in a class with the
  * reference's exact constructor and fit_transform signatures.
@@ -51,8 +52,10 @@ typedef enum ncvis_distance {
 #define NCVIS_KNN_BF16_RERANK 1 /* BF16 tensor-core distances, exact FP32 rerank */
 
 /* SGD modes (ncvis_options.sgd_mode). */
-#define NCVIS_SGD_HOGWILD 0 /* parallel chains, counter-based noise samples */
+#define NCVIS_SGD_HOGWILD 0 /* parallel chains, counter-based noise samples; staged in
+                               shared-memory windows of Y where N is large enough */
 #define NCVIS_SGD_REPLAY 1  /* one chain consuming a recorded noise stream */
+#define NCVIS_SGD_HOGWILD_UNSTAGED 2 /* parallel chains, every noise row read from Y itself */
 
 /* Constructor arguments of ncvis::NCVis (src/ncvis.hpp:54), same meaning.
  * M and ef_construction configure HNSW in the reference and are accepted and
@@ -174,6 +177,22 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
                           const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
                           int epoch_begin, int epoch_end, int n_epochs, const size_t *n_noise,
                           float a, float b, float alpha, float alpha_Q, int chains, void *stream);
+
+/* The same optimizer with its noise samples staged in shared memory
+ * (NCVis::optimize, src/ncvis.cpp:275-352, with the noise draw of :300
+ * restated): the chains run their edges in rounds of round_edges edges
+ * (0 = 8); per round each block of chains copies a window of Y (4096 rows
+ * for d <= 2, 2048 for d = 3 and 4, in segments of 256 consecutive rows,
+ * each starting at a uniform row and wrapping at N) into shared memory and draws every noise sample of the round uniformly
+ * from the window, so each noise row stays uniform over the other N - 1
+ * rows.  Updates of noise rows go to the window and are added to Y at the
+ * end of the round.  Needs 1 <= d <= 4 and N >= 16 * window rows (65,536
+ * for d <= 2, 32,768 for d = 3 and 4).  chains: 0 = automatic. */
+int ncvis_optimize_staged_device(size_t N, size_t d, size_t E, const int32_t *d_src,
+                                 const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
+                                 int epoch_begin, int epoch_end, int n_epochs,
+                                 const size_t *n_noise, float a, float b, float alpha,
+                                 float alpha_Q, int chains, int round_edges, void *stream);
 
 /* Replay: one chain runs edges [edge_begin, edge_end) of epoch `epoch` in
  * order, reading noise samples from d_stream starting at stream_offset, with

@@ -23,6 +23,7 @@ KNN_FP32 = 0
 KNN_BF16_RERANK = 1
 SGD_HOGWILD = 0
 SGD_REPLAY = 1
+SGD_HOGWILD_UNSTAGED = 2
 
 
 class NcvisParams(C.Structure):
@@ -108,6 +109,10 @@ SIGNATURES = {
     "ncvis_optimize_device": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, C.c_uint64, C.c_int,
                                         C.c_int, C.c_int, C.POINTER(_sz), C.c_float, C.c_float,
                                         C.c_float, C.c_float, C.c_int, _vp]),
+    "ncvis_optimize_staged_device": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, C.c_uint64,
+                                               C.c_int, C.c_int, C.c_int, C.POINTER(_sz),
+                                               C.c_float, C.c_float, C.c_float, C.c_float,
+                                               C.c_int, C.c_int, _vp]),
     "ncvis_optimize_replay_device": (C.c_int, [_sz, _sz, _vp, _vp, _sz, _sz, _vp, _sz, _vp, _vp,
                                                C.c_int, C.c_int, _sz, C.c_float, C.c_float,
                                                C.c_float, C.c_float, _vp]),

@@ -12,8 +12,10 @@ on the current torch stream and returns a CUDA tensor.
 
 Keyword-only extras select the engine's modes: ``knn_precision`` ("fp32",
 the plain drop-in, or "bf16" for tensor-core distances with an exact FP32
-rerank), ``rerank_factor``, ``sgd_mode`` ("hogwild" or "replay" with a
-recorded ``replay_stream``) and ``sgd_chains``.
+rerank), ``rerank_factor``, ``sgd_mode`` ("hogwild": parallel chains with the
+noise samples staged in shared-memory windows of the embedding where N is
+large enough; "hogwild_unstaged": every noise row read from the whole
+embedding; "replay" with a recorded ``replay_stream``) and ``sgd_chains``.
 """
 from __future__ import annotations
 
@@ -62,7 +64,8 @@ DISTANCES = {
 }
 
 _PRECISIONS = {"fp32": _lib.KNN_FP32, "bf16": _lib.KNN_BF16_RERANK}
-_SGD_MODES = {"hogwild": _lib.SGD_HOGWILD, "replay": _lib.SGD_REPLAY}
+_SGD_MODES = {"hogwild": _lib.SGD_HOGWILD, "replay": _lib.SGD_REPLAY,
+              "hogwild_unstaged": _lib.SGD_HOGWILD_UNSTAGED}
 
 
 class NCVis:

@@ -305,7 +305,8 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const int dist = p.distance;
     const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
     require((int64_t)N * k < (int64_t(1) << 30), "[ncvis] N * n_neighbors must be below 2^30");
-    require(host || ((uintptr_t)Y & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
+    require(host || ((uintptr_t)Y & (p.d == 4 ? 15 : 7)) == 0,
+            "[ncvis] device Y must be 8-byte aligned (16-byte for d = 4)");
     const bool replay = (o.sgd_mode == NCVIS_SGD_REPLAY);
 
     cudaStream_t s = stream();
@@ -437,7 +438,10 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(rerr == 0, "[ncvis] replay stream holds an index outside [0, N)");
     } else if (p.n_epochs > 0 && E > 0) {
-        run_sgd_hogwild(g, 0, p.n_epochs, noise.data(), chains, base + o_sgd, s);
+        if (o.sgd_mode == NCVIS_SGD_HOGWILD && sgd_window_applies(g.N, g.d))
+            run_sgd_window(g, 0, p.n_epochs, noise.data(), chains, 0, base + o_sgd, s);
+        else
+            run_sgd_hogwild(g, 0, p.n_epochs, noise.data(), chains, base + o_sgd, s);
     }
     NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
     if (host)
@@ -931,7 +935,8 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
     return guarded(nullptr, [&] {
         require(d_src && d_dst && dY && dQ && n_noise, "optimize: null pointer");
         require(N >= 2 && d >= 1 && d <= 32, "optimize: need N >= 2 and 1 <= d <= 32");
-        require(((uintptr_t)dY & 7) == 0, "optimize: Y must be 8-byte aligned");
+        require(((uintptr_t)dY & (d == 4 ? 15 : 7)) == 0,
+                "optimize: Y must be 8-byte aligned (16-byte for d = 4)");
         require((((uintptr_t)d_src | (uintptr_t)d_dst) & 15) == 0,
                 "optimize: src and dst must be 16-byte aligned");
         require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
@@ -946,6 +951,38 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
         SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,
                   a, b, alpha, alpha_Q};
         run_sgd_hogwild(g, epoch_begin, epoch_end, n_noise, chains, ws, s);
+        NCVIS_CUDA(cudaFreeAsync(ws, s));
+    });
+}
+
+int ncvis_optimize_staged_device(size_t N, size_t d, size_t E, const int32_t *d_src,
+                                 const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
+                                 int epoch_begin, int epoch_end, int n_epochs,
+                                 const size_t *n_noise, float a, float b, float alpha,
+                                 float alpha_Q, int chains, int round_edges, void *stream) {
+    return guarded(nullptr, [&] {
+        require(d_src && d_dst && dY && dQ && n_noise, "optimize_staged: null pointer");
+        require(N >= 2 && N < (size_t(1) << 31), "optimize_staged: N must be in [2, 2^31)");
+        require(sgd_window_applies((int64_t)N, (int)d),
+                "optimize_staged: needs 1 <= d <= 4 and N >= 16 * " +
+                    std::to_string(d >= 1 && d <= 4 ? sgd_window_rows((int)d) : 0u) +
+                    " (16 noise windows)");
+        require(((uintptr_t)dY & (d == 4 ? 15 : 7)) == 0,
+                "optimize_staged: Y must be 8-byte aligned (16-byte for d = 4)");
+        require((((uintptr_t)d_src | (uintptr_t)d_dst) & 15) == 0,
+                "optimize_staged: src and dst must be 16-byte aligned");
+        require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
+                "optimize_staged: need 0 <= epoch_begin <= epoch_end <= n_epochs");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (E == 0 || epoch_begin == epoch_end) return;
+        require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
+                "optimize_staged: an edge endpoint is outside [0, N)");
+        if (chains <= 0) chains = sgd_window_default_chains((int64_t)E, (int64_t)N, (int)d);
+        void *ws = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
+        SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,
+                  a, b, alpha, alpha_Q};
+        run_sgd_window(g, epoch_begin, epoch_end, n_noise, chains, round_edges, ws, s);
         NCVIS_CUDA(cudaFreeAsync(ws, s));
     });
 }

@@ -401,6 +401,277 @@ __global__ void reduce_q(const double *__restrict__ q_part, int blocks, int64_t 
     }
 }
 
+// ---------------------------------------------------------------- staged noise
+//
+// Noise samples served from a shared-memory window of Y instead of from the
+// whole array.  A block's chains run their edges in rounds; for each round
+// the block draws W / kSegRows segment starts uniformly from [0, N), copies
+// the window rows (kSegRows consecutive rows from each start, wrapping at N) into
+// shared memory with coalesced loads, and every noise sample of the round is
+// a uniform pick among the window's rows.  A row is therefore still uniform
+// over [0, N) \ {i} for every sample (the segment start is uniform and the
+// pick within the window is uniform); what changes is only that the samples
+// of one round of one block share a window.  y_o -= dx is applied to the
+// window copy; at the end of the round the window's change (current minus
+// loaded) is added to Y with coalesced L2 reductions, so updates made to the
+// same rows meanwhile by other blocks are kept.  The positive sample and y_i
+// are handled as in sgd_epoch.
+
+constexpr int kWinThreads = 512;
+constexpr uint32_t kSegRows = 256;  // rows per window segment
+
+__device__ __forceinline__ uint32_t window_row(const uint32_t *seg, uint32_t u, uint32_t N) {
+    const uint32_t r = seg[u / kSegRows] + (u % kSegRows);
+    return r >= N ? r - N : r;
+}
+
+// Segment t of round r of block b in epoch `tag`: uniform in [0, N).
+__device__ __forceinline__ uint32_t segment_start(uint32_t k0, uint32_t k1, uint32_t b, uint32_t r,
+                                                  uint32_t tag, uint32_t t, uint32_t N) {
+    const Philox4x32 x = philox4x32_10(b, r, tag, t | 0x20000000u, k0 ^ 0x3c6ef372u, k1);
+    return bounded_index(x.v[0], x.v[1], N);
+}
+
+// A noise sample whose window row is the edge source i is redrawn from
+// blocks (e_lo, e_hi ^ retry<<16, tag, s/2 | 3<<30) under key (k0 ^ retry, k1),
+// up to 64 times; then the next window row is taken.
+__device__ __forceinline__ uint32_t window_redraw(uint32_t k0, uint32_t k1, uint64_t e, uint32_t tag,
+                                                  uint32_t s, uint32_t u, uint32_t i,
+                                                  const uint32_t *seg, uint32_t W, uint32_t N) {
+    for (uint32_t retry = 1; window_row(seg, u, N) == i; ++retry) {
+        if (retry > 64) {
+            u = (u + 1 == W) ? 0 : u + 1;
+            break;
+        }
+        const Philox4x32 rr = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32) ^ (retry << 16), tag,
+                                            (s >> 1) | 0xC0000000u, k0 ^ retry, k1);
+        u = bounded_index(rr.v[2 * (s & 1)], rr.v[2 * (s & 1) + 1], W);
+    }
+    return u;
+}
+
+// Window picks of noise samples 8q .. 8q+7 of edge e: the eight 16-bit
+// halves of one Philox block (e_lo, e_hi, tag, q | 2^30), each masked to the
+// window size (a power of two <= 2^16, so every pick is exactly uniform).
+__device__ __forceinline__ Philox4x32 window_block(uint32_t k0, uint32_t k1, uint64_t e,
+                                                   uint32_t tag, uint32_t q) {
+    return philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), tag, q | 0x40000000u, k0, k1);
+}
+
+__device__ __forceinline__ uint32_t window_pick(const Philox4x32 &r, int t, uint32_t W) {
+    return (r.v[t >> 1] >> ((t & 1) * 16)) & (W - 1);
+}
+
+template <int D>
+__device__ __forceinline__ Vec<D> load_win(const float *w, uint32_t u) {
+    Vec<D> r;
+    if constexpr (D == 2) {
+        const float2 t = reinterpret_cast<const float2 *>(w)[u];
+        r.v[0] = t.x;
+        r.v[1] = t.y;
+    } else if constexpr (D == 4) {
+        const float4 t = reinterpret_cast<const float4 *>(w)[u];
+        r.v[0] = t.x;
+        r.v[1] = t.y;
+        r.v[2] = t.z;
+        r.v[3] = t.w;
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) r.v[c] = w[u * D + c];
+    }
+    return r;
+}
+
+template <int D>
+__device__ __forceinline__ void store_win(float *w, uint32_t u, const Vec<D> &r) {
+    if constexpr (D == 2) {
+        reinterpret_cast<float2 *>(w)[u] = make_float2(r.v[0], r.v[1]);
+    } else if constexpr (D == 4) {
+        reinterpret_cast<float4 *>(w)[u] = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) w[u * D + c] = r.v[c];
+    }
+}
+
+// One noise sample against window row u: y_o read from the window and
+// y_o - dx stored back, a lock-free read-modify-write like the reference's
+// (shared-memory atomics measured ~10% slower for the optimizer at 1,024,000
+// points; concurrent updates of one window row are rare).
+template <int D>
+__device__ __forceinline__ void window_sample(float *win, uint32_t u, Vec<D> &yi,
+                                              const EpochConst &k, float &Qc) {
+    const Vec<D> yo = load_win<D>(win, u);
+    const float ws = nce_weight(sq_dist<D>(yi, yo), false, k, Qc);
+    Vec<D> dx, yn;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        dx.v[c] = clip4((yo.v[c] - yi.v[c]) * ws);
+        yi.v[c] += dx.v[c];
+        yn.v[c] = yo.v[c] - dx.v[c];
+    }
+    store_win<D>(win, u, yn);
+}
+
+// Edge indices e .. e+3 (entries at or past b are -1).
+__device__ __forceinline__ void load_group(const int32_t *__restrict__ src,
+                                           const int32_t *__restrict__ dst, int64_t e, int64_t b,
+                                           int32_t (&sv)[4], int32_t (&dv)[4]) {
+    if (e + 4 <= b) {
+        const int4 s4 = __ldg(reinterpret_cast<const int4 *>(src + e));
+        const int4 d4 = __ldg(reinterpret_cast<const int4 *>(dst + e));
+        sv[0] = s4.x, sv[1] = s4.y, sv[2] = s4.z, sv[3] = s4.w;
+        dv[0] = d4.x, dv[1] = d4.y, dv[2] = d4.z, dv[3] = d4.w;
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            sv[q] = e + q < b ? src[e + q] : -1;
+            dv[q] = e + q < b ? dst[e + q] : -1;
+        }
+    }
+}
+
+// The positive rows of a group of edges (self edges and padding skipped).
+template <int D>
+__device__ __forceinline__ void gather_group(const float *Y, const int32_t (&sv)[4],
+                                             const int32_t (&dv)[4], Vec<D> (&yj)[4]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (dv[q] >= 0 && dv[q] != sv[q]) yj[q] = load_row<D>(Y, dv[q]);
+}
+
+// Edges [a, b) of a chain (a a multiple of 4) against the round's window; the
+// chain's current source row (ci, yi, valid when `have`) carries over rounds.
+// The positive rows of a group of four edges are gathered together before the
+// group runs (one memory round trip per group instead of one per edge); a
+// gathered row that this chain wrote in between (an earlier positive row or
+// a stored source of the group) is read again, so the chain always sees its
+// own updates.
+template <int D>
+__device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict__ src,
+                                             const int32_t *__restrict__ dst, int64_t a, int64_t b,
+                                             uint32_t N, const EpochConst &k, float &Qc,
+                                             uint32_t key0, uint32_t key1, uint32_t tag,
+                                             float *win, const uint32_t *seg, uint32_t W,
+                                             bool &have, uint32_t &ci, Vec<D> &yi) {
+    for (int64_t e = a; e < b; e += 4) {
+        int32_t sv[4], dv[4];
+        load_group(src, dst, e, b, sv, dv);
+        Vec<D> yj[4] = {};
+        gather_group<D>(Y, sv, dv, yj);
+        const int32_t ci0 = have ? (int32_t)ci : -1;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (e + q >= b) break;
+            const uint32_t i = (uint32_t)sv[q], j = (uint32_t)dv[q];
+            if (!have || i != ci) {
+                if (have) store_row<D>(Y, ci, yi);
+                ci = i;
+                yi = load_row<D>(Y, ci);
+                have = true;
+            }
+            if (j != i) {
+                const int32_t jj = dv[q];
+                bool stale = jj == ci0;
+#pragma unroll
+                for (int x = 0; x < q; ++x) stale |= (jj == sv[x]) | (jj == dv[x]);
+                const Vec<D> yjv = stale ? load_row<D>(Y, j) : yj[q];
+                const float ws = nce_weight(sq_dist<D>(yi, yjv), true, k, Qc);
+                Vec<D> dx;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    dx.v[c] = clip4((yjv.v[c] - yi.v[c]) * ws);
+                    yi.v[c] += dx.v[c];
+                }
+                sub_row<D>(Y, j, dx);
+            } else {
+                // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
+                const float ws = nce_weight(0.f, true, k, Qc);
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    const float dx = clip4(0.f * ws);
+                    yi.v[c] = (yi.v[c] + dx) - dx;
+                }
+            }
+            for (int s0 = 0; s0 < k.nu; s0 += 8) {
+                const Philox4x32 r = window_block(key0, key1, (uint64_t)(e + q), tag,
+                                                  (uint32_t)(s0 >> 3));
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    if (s0 + t >= k.nu) break;
+                    const uint32_t u = window_redraw(key0, key1, (uint64_t)(e + q), tag,
+                                                     (uint32_t)(s0 + t), window_pick(r, t, W), i,
+                                                     seg, W, N);
+                    window_sample<D>(win, u, yi, k, Qc);
+                }
+            }
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
+    float *__restrict__ Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
+    int64_t E, uint32_t N, const float *__restrict__ Q_in, double *__restrict__ q_part,
+    EpochConst k, int epoch, uint32_t key0, uint32_t key1, int64_t chunk, int64_t n_chains,
+    uint32_t W, int round_edges) {
+    extern __shared__ __align__(16) float win_smem[];
+    float *win = win_smem;                                    // current window rows [W][D]
+    float *loaded = win_smem + (size_t)W * D;                 // the rows as loaded [W][D]
+    uint32_t *seg = reinterpret_cast<uint32_t *>(loaded + (size_t)W * D);  // [W / kSegRows]
+    const int64_t chain = (int64_t)blockIdx.x * kWinThreads + threadIdx.x;
+    const int64_t e0 = chain < n_chains ? min(E, chain * chunk) : E;
+    const int64_t e1 = min(E, e0 + chunk);
+    const int rounds = (int)((chunk + round_edges - 1) / round_edges);
+    const uint32_t nseg = W / kSegRows;
+    float Qc = *Q_in;
+    bool have = false;
+    uint32_t ci = 0;
+    Vec<D> yi;
+#pragma unroll
+    for (int c = 0; c < D; ++c) yi.v[c] = 0.f;
+    for (int r = 0; r < rounds; ++r) {
+        for (uint32_t t = threadIdx.x; t < nseg; t += kWinThreads)
+            seg[t] = segment_start(key0, key1, blockIdx.x, (uint32_t)r, (uint32_t)epoch, t, N);
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < W; u += kWinThreads) {
+            const Vec<D> v = load_row<D>(Y, window_row(seg, u, N));
+            store_win<D>(win, u, v);
+            store_win<D>(loaded, u, v);
+        }
+        __syncthreads();
+        const int64_t a = min(e1, e0 + (int64_t)r * round_edges);
+        const int64_t b = min(e1, a + round_edges);
+        window_edges<D>(Y, src, dst, a, b, N, k, Qc, key0, key1, (uint32_t)epoch, win, seg,
+                                 W, have, ci, yi);
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < W; u += kWinThreads) {
+            const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
+            Vec<D> minus;  // loaded - current: sub_row adds current - loaded
+            bool moved = false;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                minus.v[c] = was.v[c] - now.v[c];
+                moved |= (minus.v[c] != 0.f);
+            }
+            if (moved) sub_row<D>(Y, window_row(seg, u, N), minus);
+        }
+        __syncthreads();
+    }
+    if (have) store_row<D>(Y, ci, yi);
+    __shared__ double red[kWinThreads / 32];
+    double v = chain < n_chains ? (double)Qc : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < kWinThreads / 32; ++w) t += red[w];
+        q_part[blockIdx.x] = t;
+    }
+}
+
 // ---------------------------------------------------------------- replay
 
 // The reference build's d_sqr: left to right for d <= 3; for d >= 4 four
@@ -575,6 +846,99 @@ void run_sgd_hogwild(const SgdArgs &g, int epoch_begin, int epoch_end, const siz
                              g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, total_chains);
         }
         NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, blocks, total_chains, g.Q);
+    }
+}
+
+// Window rows of the staged-noise kernel: the largest power of two, at most
+// 4096, whose two copies of D floats per row fit in 64 KiB.
+uint32_t sgd_window_rows(int d) {
+    uint32_t w = 4096;
+    while (w > kSegRows && (size_t)w * d * 8 > 65536) w >>= 1;
+    return w;
+}
+
+bool sgd_window_applies(int64_t N, int d) {
+    return d >= 1 && d <= 4 && N >= 16 * (int64_t)sgd_window_rows(d);
+}
+
+namespace {
+
+template <int D>
+void launch_window_epoch(unsigned blocks, size_t smem, cudaStream_t s, const SgdArgs &g,
+                         double *q_part, const EpochConst &k, int ep, uint32_t key0, uint32_t key1,
+                         int64_t chunk, int64_t chains, uint32_t W, int round_edges) {
+    NCVIS_CUDA(cudaFuncSetAttribute(sgd_epoch_window<D>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NCVIS_LAUNCH(sgd_epoch_window<D>, blocks, kWinThreads, smem, s, g.Y, g.src, g.dst,
+                 g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, chains, W,
+                 round_edges);
+}
+
+int64_t window_resident_chains(int d) {
+    const uint32_t W = sgd_window_rows(d);
+    const size_t smem = (size_t)W * d * 8 + (W / kSegRows) * 4;
+    int blocks = 0;
+    cudaError_t err;
+    auto occ = [&](auto kernel) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kWinThreads, smem);
+    };
+    switch (d) {
+        case 1: err = occ(sgd_epoch_window<1>); break;
+        case 2: err = occ(sgd_epoch_window<2>); break;
+        case 3: err = occ(sgd_epoch_window<3>); break;
+        default: err = occ(sgd_epoch_window<4>);
+    }
+    if (err != cudaSuccess || blocks < 1) blocks = 1;
+    return (int64_t)blocks * kWinThreads * num_sms();
+}
+
+}  // namespace
+
+int sgd_window_default_chains(int64_t E, int64_t N, int d) {
+    // As sgd_default_chains: every chain resident, at least 16 edges each, at
+    // most one chain per 2 points.
+    int64_t chains = std::min<int64_t>(window_resident_chains(d), std::max<int64_t>(E / 16, 1));
+    chains = std::min<int64_t>(chains, std::max<int64_t>(N / 2, 1));
+    return (int)std::max<int64_t>(chains, 1);
+}
+
+void run_sgd_window(const SgdArgs &g, int epoch_begin, int epoch_end, const size_t *n_noise,
+                    int chains, int round_edges, void *workspace, cudaStream_t s) {
+    require(g.N >= 2 && g.N < (int64_t(1) << 31), "optimize: N must be in [2, 2^31)");
+    require(sgd_window_applies(g.N, g.d),
+            "optimize: staged noise needs 1 <= d <= 4 and N >= 16 window rows");
+    if (chains <= 0) chains = sgd_window_default_chains(g.E, g.N, g.d);
+    if (round_edges <= 0) round_edges = 16;
+    round_edges = (round_edges + 3) & ~3;
+    const uint32_t W = sgd_window_rows(g.d);
+    const size_t smem = (size_t)W * g.d * 8 + (W / kSegRows) * 4;
+    const unsigned blocks = ceil_div(chains, kWinThreads);
+    const int64_t total_chains = chains;
+    const int64_t chunk = ((g.E + total_chains - 1) / total_chains + 3) & ~(int64_t)3;
+    double *q_part = (double *)workspace;
+    uint32_t key0, key1;
+    noise_key(g.seed, key0, key1);
+    for (int ep = epoch_begin; ep < epoch_end; ++ep) {
+        EpochConst k = epoch_const(g, ep, (int)n_noise[ep]);
+        switch (g.d) {
+            case 1:
+                launch_window_epoch<1>(blocks, smem, s, g, q_part, k, ep, key0, key1,
+                                                   chunk, total_chains, W, round_edges);
+                break;
+            case 2:
+                launch_window_epoch<2>(blocks, smem, s, g, q_part, k, ep, key0, key1,
+                                                   chunk, total_chains, W, round_edges);
+                break;
+            case 3:
+                launch_window_epoch<3>(blocks, smem, s, g, q_part, k, ep, key0, key1,
+                                                   chunk, total_chains, W, round_edges);
+                break;
+            default:
+                launch_window_epoch<4>(blocks, smem, s, g, q_part, k, ep, key0, key1,
+                                                   chunk, total_chains, W, round_edges);
+        }
+        NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, (int)blocks, total_chains, g.Q);
     }
 }
 

@@ -120,6 +120,13 @@ size_t sgd_workspace_bytes(int chains);
 int sgd_default_chains(int64_t E, int64_t N, int d);
 void run_sgd_hogwild(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
                      int chains, void *workspace, cudaStream_t s);
+// Hogwild with noise staged in shared-memory windows of Y (d <= 4, N >= 16
+// window rows); round_edges <= 0: the default (8 edges per chain per round).
+uint32_t sgd_window_rows(int d);
+bool sgd_window_applies(int64_t N, int d);
+int sgd_window_default_chains(int64_t E, int64_t N, int d);
+void run_sgd_window(const SgdArgs &args, int epoch_begin, int epoch_end, const size_t *n_noise,
+                    int chains, int round_edges, void *workspace, cudaStream_t s);
 // Batched Hogwild: problem p owns rows [off[p], off[p+1]), edges
 // [eoff[p], eoff[p+1]) and chains [cp[p], cp[p+1]) (device arrays); Qs[B] and
 // chain_q[n_chains] device floats.  d <= 4.

@@ -84,9 +84,11 @@ def init_embedding(row_ptr, cols, d: int, seed: int, n_init_epochs: int, alpha: 
 
 
 def optimize(Y, Q, src, dst, seed: int, n_noise, a: float, b: float, alpha: float = 1.0,
-             alpha_Q: float = 1.0, epoch_begin: int = 0, epoch_end=None, chains: int = 0):
+             alpha_Q: float = 1.0, epoch_begin: int = 0, epoch_end=None, chains: int = 0,
+             staged: bool = False, round_edges: int = 0):
     """Hogwild NCE SGD in place on Y (CUDA float32 [N, d]) and Q (CUDA float32
-    scalar tensor); returns (Y, Q)."""
+    scalar tensor); returns (Y, Q).  staged=True draws the noise samples from
+    shared-memory windows of Y (ncvis_optimize_staged_device)."""
     plan = np.ascontiguousarray(n_noise, dtype=np.uintp)
     n_epochs = plan.shape[0]
     if epoch_end is None:
@@ -95,10 +97,17 @@ def optimize(Y, Q, src, dst, seed: int, n_noise, a: float, b: float, alpha: floa
     N, d = Y.shape
     assert Y.is_contiguous() and Y.dtype == _torch().float32
     arr = (C.c_size_t * max(1, n_epochs))(*[int(v) for v in plan])
-    _lib.check(_lib.lib().ncvis_optimize_device(N, d, src.shape[0], src.data_ptr(),
-                                                dst.data_ptr(), Y.data_ptr(), Q.data_ptr(), seed,
-                                                epoch_begin, epoch_end, n_epochs, arr, a, b, alpha,
-                                                alpha_Q, chains, _stream()))
+    L = _lib.lib()
+    if staged:
+        rc = L.ncvis_optimize_staged_device(N, d, src.shape[0], src.data_ptr(), dst.data_ptr(),
+                                            Y.data_ptr(), Q.data_ptr(), seed, epoch_begin,
+                                            epoch_end, n_epochs, arr, a, b, alpha, alpha_Q,
+                                            chains, round_edges, _stream())
+    else:
+        rc = L.ncvis_optimize_device(N, d, src.shape[0], src.data_ptr(), dst.data_ptr(),
+                                     Y.data_ptr(), Q.data_ptr(), seed, epoch_begin, epoch_end,
+                                     n_epochs, arr, a, b, alpha, alpha_Q, chains, _stream())
+    _lib.check(rc)
     return Y, Q
 
 
