@@ -6,7 +6,8 @@ or 64 (rerank_factor 4: the 4k = 60 the headline configuration names), and the
 rerank restores the exact FP32 distances and the reference's row contract.  Bar: recall@15
 against FP64 exact search >= 0.99 (the 131,072 x 100 vMF configuration is
 checked on a 2000-query subsample), every returned distance equal to the
-FP32 distance of its pair to 1e-5 relative, rows in descending order."""
+FP32 distance of its pair to 1e-5 relative, rows in descending order.  All four
+distances are checked the same way at 131,072 x 64 (2000-query sample)."""
 import numpy as np
 import pytest
 
@@ -70,6 +71,30 @@ def test_vmf_131072_recall_64_candidates(cuda, oracle):
     print(f"recall@15 (64 candidates): {r:.5f}")
     assert r >= 0.99
     assert np.all(np.diff(gd, axis=1) <= 0)
+
+
+@pytest.mark.parametrize("dist", [0, 1, 2, 3])
+def test_distances_131072(cuda, oracle, dist):
+    """All four distances at 131,072 x 64 on a Gaussian mixture whose
+    components sit at different offsets and scales, so that squared L2, inner
+    product, cosine and correlation rank differently (squared L2 runs the
+    folded-norm product)."""
+    rng = np.random.default_rng(20 + dist)
+    X, lab = gmm(131072, 64, 24, 4.0, seed=30 + dist)
+    X = (X * rng.uniform(0.5, 2.0, size=24)[lab][:, None] + 3.0).astype(np.float32)
+    gi, gd = _knn(cuda, X, 15, dist)
+    q = np.sort(rng.choice(131072, 2000, replace=False))
+    Xp = oracle.preprocess(X, dist)
+    exact = _fp64_rows(Xp, q, 15, dist)
+    r = _recall(gi[q], exact)
+    print(f"recall@15 (BF16 + FP32 rerank, 131072 x 64, distance {dist}): {r:.5f}")
+    assert r >= 0.99, r
+    assert np.all(np.diff(gd, axis=1) <= 0)
+    for i in q[::50]:
+        for j in range(15):
+            a, b = Xp[i].astype(np.float64), Xp[gi[i, j]].astype(np.float64)
+            ref = ((a - b) ** 2).sum() if dist == 0 else 1.0 - (a * b).sum()
+            assert abs(gd[i, j] - ref) <= 1e-5 * max(1.0, abs(ref))
 
 
 @pytest.mark.parametrize("dist", [0, 1, 2, 3])
