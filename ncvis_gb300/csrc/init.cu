@@ -75,6 +75,59 @@ __global__ void __launch_bounds__(kThreads) spmm_rows(int64_t N, int d,
     block_partial(sums, d, part);
 }
 
+// spmm_rows for d <= 4: the column indices and rows of eight edges are
+// loaded together before they are added in CSR order (the same sums, one
+// memory round trip per eight edges instead of two per edge).
+template <int D>
+__global__ void __launch_bounds__(kThreads) spmm_rows_d(int64_t N, const int64_t *__restrict__ row_ptr,
+                                                        const int32_t *__restrict__ cols,
+                                                        float alpha, const float *__restrict__ Yold,
+                                                        float *__restrict__ Ynew,
+                                                        double *__restrict__ part) {
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    double sums[kMaxDim];
+#pragma unroll
+    for (int c = 0; c < D; ++c) sums[c] = 0;
+    if (i < N) {
+        float acc[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = 0.f;
+        const int64_t p0 = row_ptr[i], p1 = row_ptr[i + 1];
+        for (int64_t p = p0; p < p1; p += 8) {
+            int32_t cc[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cc[k] = (p + k < p1) ? __ldg(cols + p + k) : -1;
+            float yv[8][D];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (cc[k] >= 0) {
+                    if constexpr (D == 2) {
+                        const float2 t = __ldg(reinterpret_cast<const float2 *>(Yold) + cc[k]);
+                        yv[k][0] = t.x;
+                        yv[k][1] = t.y;
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < D; ++c) yv[k][c] = __ldg(Yold + (int64_t)cc[k] * D + c);
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (cc[k] >= 0) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c)
+                        acc[c] = __fadd_rn(acc[c], __fmul_rn(alpha, yv[k][c]));
+                }
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            Ynew[i * D + c] = acc[c];
+            sums[c] = acc[c];
+        }
+    }
+    block_partial(sums, D, part);
+}
+
 __global__ void __launch_bounds__(kThreads) centred_squares(int64_t N, int d,
                                                             const float *__restrict__ Y,
                                                             const float *__restrict__ mean,
@@ -289,8 +342,27 @@ void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t 
     for (int ep = 0; ep < n_init_epochs; ++ep) {
         const float *y_old = bufs[ep % 2];
         float *y_new = bufs[(ep + 1) % 2];
-        NCVIS_LAUNCH(spmm_rows, (unsigned)blocks, kThreads, 0, s, N, d, row_ptr, cols, alpha, y_old,
-                     y_new, part);
+        switch (d) {
+            case 1:
+                NCVIS_LAUNCH(spmm_rows_d<1>, (unsigned)blocks, kThreads, 0, s, N, row_ptr, cols,
+                             alpha, y_old, y_new, part);
+                break;
+            case 2:
+                NCVIS_LAUNCH(spmm_rows_d<2>, (unsigned)blocks, kThreads, 0, s, N, row_ptr, cols,
+                             alpha, y_old, y_new, part);
+                break;
+            case 3:
+                NCVIS_LAUNCH(spmm_rows_d<3>, (unsigned)blocks, kThreads, 0, s, N, row_ptr, cols,
+                             alpha, y_old, y_new, part);
+                break;
+            case 4:
+                NCVIS_LAUNCH(spmm_rows_d<4>, (unsigned)blocks, kThreads, 0, s, N, row_ptr, cols,
+                             alpha, y_old, y_new, part);
+                break;
+            default:
+                NCVIS_LAUNCH(spmm_rows, (unsigned)blocks, kThreads, 0, s, N, d, row_ptr, cols,
+                             alpha, y_old, y_new, part);
+        }
         NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 0, mean);
         NCVIS_LAUNCH(centred_squares, (unsigned)blocks, kThreads, 0, s, N, d, y_new, mean, part);
         NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 1, sigma);
