@@ -12,6 +12,7 @@
  *   ncvis_fit_transform          <- ncvis::NCVis::fit_transform src/ncvis.hpp:66, src/ncvis.cpp:354-459
  *   ncvis_distance               <- enum ncvis::Distance        src/ncvis.hpp:27-32
  *   ncvis_knn_device             <- NCVis::buildKNN + findKNN   src/ncvis.cpp:72-153
+ *   ncvis_knn_ivf_device         <- NCVis::buildKNN + findKNN (approximate) src/ncvis.cpp:72-153
  *   ncvis_symmetrize_device      <- KNNTable::symmetrize + NCVis::build_edges
  *                                   src/knntable.cpp:24-99, src/ncvis.cpp:155-173
  *   ncvis_init_embedding_device  <- NCVis::init_embedding       src/ncvis.cpp:184-273
@@ -50,6 +51,8 @@ typedef enum ncvis_distance {
 /* kNN precision modes (ncvis_options.knn_precision). */
 #define NCVIS_KNN_FP32 0      /* exact FP32 distances: the plain drop-in form */
 #define NCVIS_KNN_BF16_RERANK 1 /* BF16 tensor-core distances, exact FP32 rerank */
+#define NCVIS_KNN_IVF 2 /* approximate: k-means cells, each searched against its nearest cells
+                           with BF16 tensor-core distances, exact FP32 rerank */
 
 /* SGD modes (ncvis_options.sgd_mode). */
 #define NCVIS_SGD_HOGWILD 0 /* parallel chains, counter-based noise samples; staged in
@@ -81,13 +84,16 @@ typedef struct ncvis_params {
 /* Engine options beyond the reference's constructor (all zero = defaults:
  * FP32 exact kNN, Hogwild SGD, engine-owned stream, automatic chain count). */
 typedef struct ncvis_options {
-    int knn_precision;      /* NCVIS_KNN_FP32 | NCVIS_KNN_BF16_RERANK */
+    int knn_precision;      /* NCVIS_KNN_FP32 | NCVIS_KNN_BF16_RERANK | NCVIS_KNN_IVF */
     int rerank_factor;      /* candidates kept per point ~ rerank_factor * k (0: 2; BF16 keeps 32 or 64) */
     int sgd_mode;           /* NCVIS_SGD_HOGWILD | NCVIS_SGD_REPLAY */
     const int32_t *replay_stream; /* host array of noise indices in one-thread draw order (replay) */
     size_t replay_len;      /* entries in replay_stream: E * sum(n_noise) */
     void *stream;           /* cudaStream_t to run on; NULL: the engine's own stream */
     int sgd_chains;         /* parallel SGD chains; 0: automatic */
+    int ivf_lists;          /* NCVIS_KNN_IVF: k-means cells; 0: N / 512 (at most 65,536) */
+    int ivf_probe;          /* NCVIS_KNN_IVF: cells searched per cell, its own included, at
+                               most 64; 0: 32 */
 } ncvis_options;
 
 /* Per-stage device times of the last fit_transform, in milliseconds, named
@@ -152,6 +158,15 @@ int ncvis_get_stage_times(ncvis_handle h, ncvis_stage_times *out);
  * (centring for correlation, unit norm for cosine/correlation). */
 int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
                      int rerank_factor, int32_t *d_inds, float *d_dists, void *stream);
+
+/* The approximate kNN of NCVIS_KNN_IVF with explicit cells and probes (0:
+ * the defaults); the row contract and distances as ncvis_knn_device.  The
+ * reference's kNN (hnswlib, src/ncvis.cpp:72-153) is approximate too; this
+ * is the GPU counterpart for point counts where the exact search's O(N^2 D)
+ * work is too large.  Needs D <= 128 (D <= 126 for squared L2). */
+int ncvis_knn_ivf_device(const float *dX, size_t N, size_t D, int distance, size_t k,
+                         int rerank_factor, int lists, int probe, int32_t *d_inds,
+                         float *d_dists, void *stream);
 
 /* Symmetrization, bit-exact with the reference's one-thread
  * KNNTable::symmetrize on the same table, emitted as CSR.  Rows are the

@@ -21,6 +21,7 @@ NCVIS_INTERNAL = 5
 
 KNN_FP32 = 0
 KNN_BF16_RERANK = 1
+KNN_IVF = 2
 SGD_HOGWILD = 0
 SGD_REPLAY = 1
 SGD_HOGWILD_UNSTAGED = 2
@@ -54,6 +55,8 @@ class NcvisOptions(C.Structure):
         ("replay_len", C.c_size_t),
         ("stream", C.c_void_p),
         ("sgd_chains", C.c_int),
+        ("ivf_lists", C.c_int),
+        ("ivf_probe", C.c_int),
     ]
 
 
@@ -102,6 +105,8 @@ SIGNATURES = {
     "ncvis_get_last_error": (C.c_char_p, []),
     "ncvis_get_stage_times": (C.c_int, [_vp, C.POINTER(NcvisStageTimes)]),
     "ncvis_knn_device": (C.c_int, [_vp, _sz, _sz, C.c_int, _sz, C.c_int, C.c_int, _vp, _vp, _vp]),
+    "ncvis_knn_ivf_device": (C.c_int, [_vp, _sz, _sz, C.c_int, _sz, C.c_int, C.c_int, C.c_int,
+                                       _vp, _vp, _vp]),
     "ncvis_symmetrize_device": (C.c_int, [_sz, _sz, _vp, _vp, _vp, _vp, _vp, _vp,
                                           C.POINTER(_sz), _vp]),
     "ncvis_init_embedding_device": (C.c_int, [_sz, _sz, _vp, _vp, C.c_uint64, C.c_int, C.c_float,

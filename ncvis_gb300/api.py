@@ -11,8 +11,10 @@ entry point; a CUDA torch tensor runs through the device-buffer entry point
 on the current torch stream and returns a CUDA tensor.
 
 Keyword-only extras select the engine's modes: ``knn_precision`` ("fp32",
-the plain drop-in, or "bf16" for tensor-core distances with an exact FP32
-rerank), ``rerank_factor``, ``sgd_mode`` ("hogwild": parallel chains with the
+the plain drop-in; "bf16" for tensor-core distances with an exact FP32
+rerank; "ivf" for the approximate search over k-means cells, with
+``ivf_lists`` cells and ``ivf_probe`` cells searched per cell, 0 = defaults),
+``rerank_factor``, ``sgd_mode`` ("hogwild": parallel chains with the
 noise samples staged in shared-memory windows of the embedding where N is
 large enough; "hogwild_unstaged": every noise row read from the whole
 embedding; "replay" with a recorded ``replay_stream``) and ``sgd_chains``.
@@ -63,7 +65,7 @@ DISTANCES = {
     "inner_product": 1,  # inner_product
 }
 
-_PRECISIONS = {"fp32": _lib.KNN_FP32, "bf16": _lib.KNN_BF16_RERANK}
+_PRECISIONS = {"fp32": _lib.KNN_FP32, "bf16": _lib.KNN_BF16_RERANK, "ivf": _lib.KNN_IVF}
 _SGD_MODES = {"hogwild": _lib.SGD_HOGWILD, "replay": _lib.SGD_REPLAY,
               "hogwild_unstaged": _lib.SGD_HOGWILD_UNSTAGED}
 
@@ -73,7 +75,7 @@ class NCVis:
                  random_seed=42, n_epochs=50, n_init_epochs=20, spread=1., min_dist=0.4, a=None,
                  b=None, alpha=1., alpha_Q=1., n_noise=None, distance="euclidean", *,
                  knn_precision="fp32", rerank_factor=0, sgd_mode="hogwild", replay_stream=None,
-                 sgd_chains=0):
+                 sgd_chains=0, ivf_lists=0, ivf_probe=0):
         """Creates a new NCVis instance; arguments as in the reference
         (wrapper/ncvis.pyx:49-101).  M and ef_construction configure HNSW in
         the reference and are accepted and ignored (the kNN here is exact);
@@ -112,6 +114,8 @@ class NCVis:
             raise ValueError(f"knn_precision must be one of {sorted(_PRECISIONS)}")
         if sgd_mode not in _SGD_MODES:
             raise ValueError(f"sgd_mode must be one of {sorted(_SGD_MODES)}")
+        if int(ivf_lists) < 0 or int(ivf_probe) < 0:
+            raise ValueError("ivf_lists and ivf_probe must be non-negative")
 
         self.n_epochs = int(n_epochs)
         self.noise_plan = np.ascontiguousarray(negative_plan, dtype=np.uintp)
@@ -131,7 +135,8 @@ class NCVis:
             replay_stream=(self._replay.ctypes.data_as(C.POINTER(C.c_int32))
                            if self._replay is not None else None),
             replay_len=0 if self._replay is None else int(self._replay.size),
-            stream=None, sgd_chains=int(sgd_chains))
+            stream=None, sgd_chains=int(sgd_chains), ivf_lists=int(ivf_lists),
+            ivf_probe=int(ivf_probe))
         L = _lib.lib()
         self._h = L.ncvis_create(C.byref(self._params), C.byref(self._options))
         if not self._h:

@@ -167,7 +167,7 @@ static bool reads_pageable_host_memory() {
 struct BatchedTcWork {
     std::vector<int64_t> pad;     // B + 1 padded row offsets
     std::vector<int64_t> begin;   // ctas + 1
-    std::vector<int4> items;
+    std::vector<TcItem> items;
     int ctas = 0;
 };
 
@@ -178,7 +178,7 @@ static BatchedTcWork plan_batched_tc(const std::vector<int64_t> &off, int ctas_m
     w.pad[0] = 0;
     struct Tile {
         int64_t cost;
-        int4 item;
+        TcItem item;
     };
     std::vector<Tile> tiles;
     for (size_t p = 0; p < B; ++p) {
@@ -186,13 +186,14 @@ static BatchedTcWork plan_batched_tc(const std::vector<int64_t> &off, int ctas_m
         w.pad[p + 1] = w.pad[p] + (n + 255) / 256 * 256;
         const int64_t cost = (n + 127) / 128;
         for (int64_t t = 0; t * 256 < n; ++t)
-            tiles.push_back({cost, make_int4((int)(w.pad[p] + 256 * t), (int)w.pad[p],
-                                             (int)(w.pad[p] + n), (int)(off[p] - w.pad[p]))});
+            tiles.push_back({cost, TcItem{(int)(w.pad[p] + 256 * t), (int)(w.pad[p] + n),
+                                          (int)w.pad[p], (int)(w.pad[p] + n),
+                                          (int)(off[p] - w.pad[p]), 0, 0, 0}});
     }
     std::stable_sort(tiles.begin(), tiles.end(),
                      [](const Tile &a, const Tile &b) { return a.cost > b.cost; });
     w.ctas = (int)std::min<int64_t>((int64_t)tiles.size(), ctas_max);
-    std::vector<std::vector<int4>> per(w.ctas);
+    std::vector<std::vector<TcItem>> per(w.ctas);
     std::vector<int64_t> load(w.ctas, 0);
     for (const Tile &t : tiles) {
         const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
@@ -303,7 +304,8 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const int k = (int)kk;
     const int d = (int)p.d;
     const int dist = p.distance;
-    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
+    const bool ivf = (o.knn_precision == NCVIS_KNN_IVF);
+    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK) || ivf;
     require((int64_t)N * k < (int64_t(1) << 30), "[ncvis] N * n_neighbors must be below 2^30");
     require(host || ((uintptr_t)Y & (p.d == 4 ? 15 : 7)) == 0,
             "[ncvis] device Y must be 8-byte aligned (16-byte for d = 4)");
@@ -379,7 +381,11 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
-    if (bf16)
+    if (ivf)
+        run_knn_ivf(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist,
+                    plan_ivf((int64_t)N, o.ivf_lists, o.ivf_probe), (uint64_t)p.random_seed,
+                    cand_i, flag + 2, s);
+    else if (bf16)
         launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s, nullptr,
                              Xc);
     else
@@ -479,7 +485,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     require(p.distance >= 0 && p.distance <= 3,
             "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
     require(p.d >= 1 && p.d <= 4, "[ncvis] batched: embedding dimension d must be in [1, 4]");
-    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK);
+    // Batched problems are small: the IVF mode runs the exact BF16 search here.
+    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK || o.knn_precision == NCVIS_KNN_IVF);
     require(((uintptr_t)dY & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
     // k is clamped by the smallest problem (src/ncvis.cpp:381-382 per problem).
     int64_t kk = std::min<int64_t>((int64_t)p.n_neighbors, min_n - 1);
@@ -552,7 +559,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     const size_t o_sqp = bf16 ? L.take(sizeof(float) * total_pad) : 0;
     const size_t o_pad = bf16 ? L.take(sizeof(int64_t) * (B + 1)) : 0;
     const size_t o_wb = bf16 ? L.take(sizeof(int64_t) * (tw.ctas + 1)) : 0;
-    const size_t o_wi = bf16 ? L.take(sizeof(int4) * std::max<size_t>(tw.items.size(), 1)) : 0;
+    const size_t o_wi = bf16 ? L.take(sizeof(TcItem) * std::max<size_t>(tw.items.size(), 1)) : 0;
     char *base = ensure_arena(L.total);
     float *Xp = (float *)(base + o_Xp);
     float *sqn = (float *)(base + o_sqn);
@@ -597,12 +604,12 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         __nv_bfloat16 *Xb_pad = (__nv_bfloat16 *)(base + o_Xbp);
         float *sqn_pad = (float *)(base + o_sqp);
         int64_t *d_pad = (int64_t *)(base + o_pad), *d_wb = (int64_t *)(base + o_wb);
-        int4 *d_wi = (int4 *)(base + o_wi);
+        TcItem *d_wi = (TcItem *)(base + o_wi);
         NCVIS_CUDA(cudaMemcpyAsync(d_pad, tw.pad.data(), sizeof(int64_t) * (B + 1),
                                    cudaMemcpyHostToDevice, s));
         NCVIS_CUDA(cudaMemcpyAsync(d_wb, tw.begin.data(), sizeof(int64_t) * (tw.ctas + 1),
                                    cudaMemcpyHostToDevice, s));
-        NCVIS_CUDA(cudaMemcpyAsync(d_wi, tw.items.data(), sizeof(int4) * tw.items.size(),
+        NCVIS_CUDA(cudaMemcpyAsync(d_wi, tw.items.data(), sizeof(TcItem) * tw.items.size(),
                                    cudaMemcpyHostToDevice, s));
         NCVIS_CUDA(cudaMemsetAsync(Xb_pad, 0, sizeof(__nv_bfloat16) * total_pad * tp.ldb, s));
         NCVIS_CUDA(cudaMemsetAsync(sqn_pad, 0, sizeof(float) * total_pad, s));
@@ -615,7 +622,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
             NCVIS_LAUNCH(pad_rows, (unsigned)ceil_div(total * 32, 256), 256, 0, s, Xc, sqn, d_off,
                          d_pad, (int)B, total, tp.ldb, Xc_pad, sqn_pad);
         }
-        TcWork work{tw.ctas, d_wb, d_wi};
+        TcWork work{tw.ctas, d_wb, d_wi, nullptr};
         launch_knn_select_tc(Xb_pad, sqn_pad, total_pad, tp, dist, cand_i, cand_d, flag + 2, s,
                              &work, Xc_pad);
         int timeout = 0;
@@ -811,17 +818,22 @@ int ncvis_get_stage_times(ncvis_handle h, ncvis_stage_times *out) {
     return NCVIS_OK;
 }
 
-int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
-                     int rerank_factor, int32_t *d_inds, float *d_dists, void *stream) {
-    return guarded(nullptr, [&] {
+namespace {
+
+void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
+                int rerank_factor, int lists, int probe, int32_t *d_inds, float *d_dists,
+                void *stream) {
+    {
         require(dX && d_inds && d_dists, "knn: null pointer");
         require(N >= 2 && k >= 1 && k <= N - 1 && k <= 255, "knn: need 2 <= N and 1 <= k <= min(N-1, 255)");
         require(D >= 1 && N < (size_t(1) << 31) && N * k < (size_t(1) << 30),
                 "knn: need D >= 1, N < 2^31 and N * k < 2^30");
         require(distance >= 0 && distance <= 3, "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
-        require(precision == NCVIS_KNN_FP32 || precision == NCVIS_KNN_BF16_RERANK,
+        require(precision == NCVIS_KNN_FP32 || precision == NCVIS_KNN_BF16_RERANK ||
+                    precision == NCVIS_KNN_IVF,
                 "knn: unknown precision mode");
-        const bool bf16 = (precision == NCVIS_KNN_BF16_RERANK);
+        const bool ivf = (precision == NCVIS_KNN_IVF);
+        const bool bf16 = (precision == NCVIS_KNN_BF16_RERANK) || ivf;
         cudaStream_t s = (cudaStream_t)stream;
         KnnPlan kp = plan_knn_f32((int64_t)N, (int)k, rerank_factor);
         KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, (int)k, rerank_factor, distance);
@@ -854,7 +866,16 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
             throw Error(kInvalidArgument, "knn: input contains non-finite values");
         }
         NCVIS_CUDA(cudaMemsetAsync(d_inds, 0xff, sizeof(int32_t) * N * k, s));
-        if (bf16) {
+        if (ivf) {
+            try {
+                run_knn_ivf((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
+                            plan_ivf((int64_t)N, lists, probe), 42, (int32_t *)(base + o_ci),
+                            (int *)(base + o_flag) + 1, s);
+            } catch (...) {
+                cudaFreeAsync(base, s);
+                throw;
+            }
+        } else if (bf16) {
             launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
                                  (int32_t *)(base + o_ci), (float *)(base + o_cd),
                                  (int *)(base + o_flag) + 1, s, nullptr, Xc);
@@ -874,6 +895,25 @@ int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k
         launch_rerank((float *)(base + o_Xp), (int64_t)N, (int)D, distance,
                       (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s);
         NCVIS_CUDA(cudaFreeAsync(base, s));
+    }
+}
+
+}  // namespace
+
+int ncvis_knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int precision,
+                     int rerank_factor, int32_t *d_inds, float *d_dists, void *stream) {
+    return guarded(nullptr, [&] {
+        knn_device(dX, N, D, distance, k, precision, rerank_factor, 0, 0, d_inds, d_dists, stream);
+    });
+}
+
+int ncvis_knn_ivf_device(const float *dX, size_t N, size_t D, int distance, size_t k,
+                         int rerank_factor, int lists, int probe, int32_t *d_inds,
+                         float *d_dists, void *stream) {
+    return guarded(nullptr, [&] {
+        require(lists >= 0 && probe >= 0, "knn (ivf): lists and probe must be non-negative");
+        knn_device(dX, N, D, distance, k, NCVIS_KNN_IVF, rerank_factor, lists, probe, d_inds,
+                   d_dists, stream);
     });
 }
 

@@ -1,0 +1,374 @@
+// K10: approximate kNN candidate selection by an inverted-file partition, for
+// point counts where the exact O(N^2 D) selection of K2 stops being viable.
+// The reference's own kNN (hnswlib, src/ncvis.cpp:72-153) is approximate too;
+// its result contract is kept: the candidates found here go through the same
+// exact FP32 rerank (K4), so rows hold k+1 nearest-found points, the nearest
+// dropped, descending exact distances.
+//
+//   1. k-means with C cells on the BF16 copies: C initial centroids are rows
+//      drawn with Philox from the points; each pass assigns every point to its
+//      nearest centroid with the tensor-core selection kernel (queries = the
+//      points, candidates = the centroids) and moves each centroid to its
+//      cell's mean (kept when the cell is empty; unit length for cosine and
+//      correlation, whose points are unit length);
+//   2. the points are counting-sorted by cell (within a cell the order is the
+//      arrival order of the scatter's atomics) and their BF16 rows gathered
+//      in that order;
+//   3. each cell probes its own cell and the probe-1 cells whose centroids
+//      are nearest to its centroid (more while the probed cells hold fewer
+//      than R points); a work list gives every 256-row query tile of a cell
+//      one item per probed cell, consecutive items extending one tile;
+//   4. one launch of the selection kernel runs the work list over the sorted
+//      rows and writes each point's R candidates in original numbering.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "rng.cuh"
+#include "stages.cuh"
+
+namespace ncvis_gpu {
+
+namespace {
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Centroid c = row i of Xp, i drawn uniformly with Philox block (c, seed tag).
+__global__ void ivf_init(const float *__restrict__ Xp, int64_t N, int D, int C, uint32_t k0,
+                         uint32_t k1, float *__restrict__ cent) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= C) return;
+    const Philox4x32 r = philox4x32_10((uint32_t)c, 0x1f5u, 0u, 0x10000000u, k0, k1);
+    const int64_t i = bounded_index(r.v[0], r.v[1], (uint32_t)N);
+    for (int t = lane; t < D; t += 32) cent[(int64_t)c * D + t] = Xp[i * D + t];
+}
+
+// BF16 copies of the centroids in the layout of the points' copies (K1): Cq
+// on the query side and Cc on the candidate side; with the folded squared-L2
+// product Cq holds 1, 1 and Cc -|c|^2/2 (BF16 high and low part) in columns
+// D, D+1, otherwise Cc is not written (the caller passes Cc == Cq).
+__global__ void ivf_centroid_rows(const float *__restrict__ cent, int C, int D, int ldb, int fold,
+                                  __nv_bfloat16 *__restrict__ Cq, __nv_bfloat16 *__restrict__ Cc) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= C) return;
+    float sq = 0.f;
+    for (int t = lane; t < D; t += 32) {
+        const float v = cent[(int64_t)c * D + t];
+        sq += v * v;
+        Cq[(int64_t)c * ldb + t] = __float2bfloat16_rn(v);
+        if (fold) Cc[(int64_t)c * ldb + t] = __float2bfloat16_rn(v);
+    }
+    const int extra = fold ? 2 : 0;
+    for (int t = D + extra + lane; t < ldb; t += 32) {
+        Cq[(int64_t)c * ldb + t] = __float2bfloat16_rn(0.f);
+        if (fold) Cc[(int64_t)c * ldb + t] = __float2bfloat16_rn(0.f);
+    }
+    sq = warp_sum(sq);
+    if (fold && lane == 0) {
+        const float h = -0.5f * sq;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(h);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(h - __bfloat162float(hi));
+        Cq[(int64_t)c * ldb + D] = __float2bfloat16_rn(1.f);
+        Cq[(int64_t)c * ldb + D + 1] = __float2bfloat16_rn(1.f);
+        Cc[(int64_t)c * ldb + D] = hi;
+        Cc[(int64_t)c * ldb + D + 1] = lo;
+    }
+}
+
+// Cell sums and counts: point i belongs to cell cand[i * R] (its best).
+__global__ void ivf_accumulate(const float *__restrict__ Xp, int64_t N, int D,
+                               const int32_t *__restrict__ cand, int R, int C,
+                               float *__restrict__ sums, int *__restrict__ counts) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= N) return;
+    const int c = cand[i * R];
+    if (c < 0 || c >= C) return;
+    for (int t = lane; t < D; t += 32) atomicAdd(sums + (int64_t)c * D + t, Xp[i * D + t]);
+    if (lane == 0) atomicAdd(counts + c, 1);
+}
+
+// Centroids to their cells' means (unit length when `normalise`), the sums
+// and counts cleared for the next pass.
+__global__ void ivf_update(float *__restrict__ cent, float *__restrict__ sums,
+                           int *__restrict__ counts, int C, int D, int normalise) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= C) return;
+    const int n = counts[c];
+    __syncwarp();
+    if (n > 0) {
+        float sq = 0.f;
+        for (int t = lane; t < D; t += 32) {
+            const float v = sums[(int64_t)c * D + t] / (float)n;
+            sq += v * v;
+        }
+        sq = warp_sum(sq);
+        const float scale = (normalise && sq > 0.f) ? 1.f / sqrtf(sq) : 1.f;
+        for (int t = lane; t < D; t += 32)
+            cent[(int64_t)c * D + t] = sums[(int64_t)c * D + t] / (float)n * scale;
+    }
+    for (int t = lane; t < D; t += 32) sums[(int64_t)c * D + t] = 0.f;
+    __syncwarp();
+    if (lane == 0) counts[c] = 0;
+}
+
+__global__ void ivf_count(const int32_t *__restrict__ cand, int R, int64_t N, int C,
+                          int *__restrict__ counts) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int c = cand[i * R];
+    if (c >= 0 && c < C) atomicAdd(counts + c, 1);
+}
+
+__global__ void ivf_scatter(const int32_t *__restrict__ cand, int R, int64_t N, int C,
+                            const int64_t *__restrict__ starts, int *__restrict__ cursor,
+                            int32_t *__restrict__ perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int c = cand[i * R];
+    if (c < 0 || c >= C) return;
+    perm[starts[c] + atomicAdd(cursor + c, 1)] = (int32_t)i;
+}
+
+// dst[r] = src[perm[r]] for BF16 rows of ldb elements (ldb a multiple of 8).
+__global__ void ivf_gather_rows(const __nv_bfloat16 *__restrict__ src,
+                                const int32_t *__restrict__ perm, int64_t N, int ldb,
+                                __nv_bfloat16 *__restrict__ dst) {
+    const int per = ldb / 8;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * per) return;
+    const int64_t row = t / per;
+    const int v = (int)(t % per);
+    reinterpret_cast<uint4 *>(dst)[row * per + v] =
+        reinterpret_cast<const uint4 *>(src)[(int64_t)perm[row] * per + v];
+}
+
+// Work list of `nq` query rows in tiles of 256 against candidates [0, nc),
+// tiles dealt round-robin over at most num_sms() CTAs.
+struct HostWork {
+    std::vector<int64_t> begin;
+    std::vector<TcItem> items;
+    int ctas = 0;
+};
+
+HostWork all_pairs_work(int64_t nq, int64_t nc) {
+    HostWork w;
+    const int64_t tiles = (nq + 255) / 256;
+    w.ctas = (int)std::min<int64_t>(tiles, num_sms());
+    w.begin.assign(w.ctas + 1, 0);
+    for (int b = 0; b < w.ctas; ++b) {
+        for (int64_t t = b; t < tiles; t += w.ctas)
+            w.items.push_back(TcItem{(int)(256 * t), (int)nq, 0, (int)nc, 0, 0, 0, 0});
+        w.begin[b + 1] = (int64_t)w.items.size();
+    }
+    return w;
+}
+
+// Device copies of a work list (stream-ordered allocations, freed by the caller).
+struct DeviceWork {
+    int64_t *begin = nullptr;
+    TcItem *items = nullptr;
+};
+
+DeviceWork upload(const HostWork &w, cudaStream_t s) {
+    DeviceWork d;
+    NCVIS_CUDA(cudaMallocAsync((void **)&d.begin, sizeof(int64_t) * w.begin.size(), s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&d.items, sizeof(TcItem) * std::max<size_t>(w.items.size(), 1), s));
+    NCVIS_CUDA(cudaMemcpyAsync(d.begin, w.begin.data(), sizeof(int64_t) * w.begin.size(),
+                               cudaMemcpyHostToDevice, s));
+    if (!w.items.empty())
+        NCVIS_CUDA(cudaMemcpyAsync(d.items, w.items.data(), sizeof(TcItem) * w.items.size(),
+                                   cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+void release(DeviceWork &d, cudaStream_t s) {
+    if (d.begin) cudaFreeAsync(d.begin, s);
+    if (d.items) cudaFreeAsync(d.items, s);
+    d = DeviceWork{};
+}
+
+void check_timeout(int *flag, cudaStream_t s) {
+    int timeout = 0;
+    NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    require(timeout == 0, "knn (ivf): the tensor-core kernel timed out waiting on a barrier",
+            kDeviceTimeout);
+}
+
+}  // namespace
+
+IvfPlan plan_ivf(int64_t N, int lists, int probe) {
+    IvfPlan p;
+    int64_t c = lists > 0 ? lists : N / 512;
+    c = std::max<int64_t>(1, std::min<int64_t>({c, N, 65536}));
+    p.C = (int)c;
+    p.probe = std::max(1, std::min(probe > 0 ? probe : 32, std::min(p.C, 64)));
+    p.iters = 4;
+    return p;
+}
+
+void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc, int64_t N,
+                 int D, const KnnTcPlan &tp, int dist, const IvfPlan &ip, uint64_t seed,
+                 int32_t *cand_i, int *timeout_flag, cudaStream_t s) {
+    require(tp.fold || dist != kSquaredL2,
+            "knn (ivf): squared L2 needs D <= 126 (the folded-norm product)", kUnsupported);
+    require(N < (int64_t(1) << 31), "knn (ivf): N must be below 2^31");
+    const bool fold = tp.fold;
+    const int C = ip.C, ldb = tp.ldb;
+    const int Rp = ip.probe > 32 ? 64 : 32;  // nearest cells listed per cell
+    float *cent = nullptr, *sums = nullptr;
+    int *counts = nullptr, *cursor = nullptr;
+    __nv_bfloat16 *Cq = nullptr, *Cc = nullptr, *Xs = nullptr, *Xcs = nullptr;
+    int32_t *pcand = nullptr, *perm = nullptr;
+    int64_t *d_starts = nullptr;
+    NCVIS_CUDA(cudaMallocAsync((void **)&cent, sizeof(float) * C * D, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&sums, sizeof(float) * C * D, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&counts, sizeof(int) * C, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&cursor, sizeof(int) * C, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&Cq, sizeof(__nv_bfloat16) * C * ldb, s));
+    if (fold) NCVIS_CUDA(cudaMallocAsync((void **)&Cc, sizeof(__nv_bfloat16) * C * ldb, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&pcand, sizeof(int32_t) * C * Rp, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&perm, sizeof(int32_t) * N, s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&d_starts, sizeof(int64_t) * (C + 1), s));
+    NCVIS_CUDA(cudaMallocAsync((void **)&Xs, sizeof(__nv_bfloat16) * N * ldb, s));
+    if (fold) NCVIS_CUDA(cudaMallocAsync((void **)&Xcs, sizeof(__nv_bfloat16) * N * ldb, s));
+    const __nv_bfloat16 *Ccand = fold ? Cc : Cq;
+
+    // 1. k-means: ip.iters moves of the centroids, each after an assignment.
+    uint32_t k0, k1;
+    noise_key(seed ^ 0x1f51f51full, k0, k1);
+    const unsigned warps_c = ceil_div((size_t)C, 8);
+    NCVIS_LAUNCH(ivf_init, warps_c, 256, 0, s, Xp, N, D, C, k0, k1, cent);
+    NCVIS_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * C * D, s));
+    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
+    KnnTcPlan ap = tp;
+    ap.R = 32;
+    const HostWork aw = all_pairs_work(N, C);
+    DeviceWork adw = upload(aw, s);
+    const TcWork awork{aw.ctas, adw.begin, adw.items, nullptr};
+    const int normalise = (dist == kCosine || dist == kCorrelation) ? 1 : 0;
+    for (int pass = 0;; ++pass) {
+        NCVIS_LAUNCH(ivf_centroid_rows, warps_c, 256, 0, s, cent, C, D, ldb, fold ? 1 : 0, Cq,
+                     fold ? Cc : Cq);
+        launch_knn_select_tc_pair(Xb, N, Ccand, C, nullptr, ap, true, cand_i, timeout_flag, s,
+                                  awork);
+        if (pass == ip.iters) break;
+        NCVIS_LAUNCH(ivf_accumulate, (unsigned)ceil_div((size_t)N, 8), 256, 0, s, Xp, N, D, cand_i,
+                     32, C, sums, counts);
+        NCVIS_LAUNCH(ivf_update, warps_c, 256, 0, s, cent, sums, counts, C, D, normalise);
+    }
+    release(adw, s);
+    check_timeout(timeout_flag, s);
+
+    // Nearest cells of each cell (its own first for the spaces where a
+    // centroid is its own best match; the work list adds it where not).
+    const HostWork pw = all_pairs_work(C, C);
+    DeviceWork pdw = upload(pw, s);
+    KnnTcPlan pp = tp;
+    pp.R = Rp;
+    launch_knn_select_tc_pair(Cq, C, Ccand, C, nullptr, pp, true, pcand, timeout_flag, s,
+                              TcWork{pw.ctas, pdw.begin, pdw.items, nullptr});
+    release(pdw, s);
+
+    // 2. Counting sort by cell.
+    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
+    NCVIS_LAUNCH(ivf_count, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand_i, 32, N, C,
+                 counts);
+    std::vector<int> h_counts(C);
+    std::vector<int32_t> h_pcand((size_t)C * Rp);
+    NCVIS_CUDA(cudaMemcpyAsync(h_counts.data(), counts, sizeof(int) * C, cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaMemcpyAsync(h_pcand.data(), pcand, sizeof(int32_t) * C * Rp,
+                               cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    check_timeout(timeout_flag, s);
+    std::vector<int64_t> starts(C + 1, 0);
+    for (int c = 0; c < C; ++c) starts[c + 1] = starts[c] + h_counts[c];
+    require(starts[C] == N, "knn (ivf): a point was not assigned to a cell", kInternal);
+    NCVIS_CUDA(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * (C + 1),
+                               cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * C, s));
+    NCVIS_LAUNCH(ivf_scatter, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand_i, 32, N, C,
+                 d_starts, cursor, perm);
+    const size_t vec = (size_t)N * (ldb / 8);
+    NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xb, perm, N, ldb, Xs);
+    if (fold)
+        NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xc, perm, N, ldb,
+                     Xcs);
+
+    // 3. Work list: every 256-row query tile of a cell, one item per probed cell.
+    struct Tile {
+        int64_t cost;
+        std::vector<TcItem> items;
+    };
+    std::vector<Tile> tiles;
+    std::vector<char> taken(C, 0);
+    for (int c = 0; c < C; ++c) {
+        if (h_counts[c] == 0) continue;
+        std::vector<int> probes{c};
+        taken[c] = 1;
+        int64_t have = h_counts[c];
+        auto add = [&](int p) {
+            if (p < 0 || p >= C || taken[p] || h_counts[p] == 0) return;
+            probes.push_back(p);
+            taken[p] = 1;
+            have += h_counts[p];
+        };
+        for (int j = 0; j < Rp && (int)probes.size() < ip.probe; ++j) add(h_pcand[(size_t)c * Rp + j]);
+        for (int j = 0; j < Rp && have < tp.R; ++j) add(h_pcand[(size_t)c * Rp + j]);
+        for (int p = 0; p < C && have < tp.R; ++p) add(p);
+        for (int p : probes) taken[p] = 0;
+        int64_t cost = 0;
+        for (int p : probes) cost += (h_counts[p] + 127) / 128 + 1;
+        const int64_t a = starts[c], n = h_counts[c];
+        for (int64_t t = 0; t * 256 < n; ++t) {
+            Tile tile{cost, {}};
+            for (size_t idx = 0; idx < probes.size(); ++idx) {
+                const int p = probes[idx];
+                int flags = 0;
+                if (idx > 0) flags |= kTcContinue;
+                if (idx + 1 < probes.size()) flags |= kTcMore;
+                tile.items.push_back(TcItem{(int)(a + 256 * t), (int)(a + n), (int)starts[p],
+                                            (int)(starts[p] + h_counts[p]), 0, flags, 0, 0});
+            }
+            tiles.push_back(std::move(tile));
+        }
+    }
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const Tile &x, const Tile &y) { return x.cost > y.cost; });
+    HostWork sw;
+    sw.ctas = (int)std::min<int64_t>((int64_t)tiles.size(), num_sms());
+    std::vector<std::vector<const Tile *>> per(sw.ctas);
+    std::vector<int64_t> load(sw.ctas, 0);
+    for (const Tile &t : tiles) {
+        const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        per[b].push_back(&t);
+        load[b] += t.cost;
+    }
+    sw.begin.assign(sw.ctas + 1, 0);
+    for (int b = 0; b < sw.ctas; ++b) {
+        for (const Tile *t : per[b]) sw.items.insert(sw.items.end(), t->items.begin(), t->items.end());
+        sw.begin[b + 1] = (int64_t)sw.items.size();
+    }
+
+    // 4. The search over the sorted rows, written in original numbering.
+    DeviceWork sdw = upload(sw, s);
+    launch_knn_select_tc_pair(Xs, N, fold ? Xcs : Xs, N, nullptr, tp, true, cand_i, timeout_flag,
+                              s, TcWork{sw.ctas, sdw.begin, sdw.items, perm});
+    release(sdw, s);
+    check_timeout(timeout_flag, s);
+    for (void *ptr : {(void *)cent, (void *)sums, (void *)counts, (void *)cursor, (void *)Cq,
+                      (void *)Cc, (void *)pcand, (void *)perm, (void *)d_starts, (void *)Xs,
+                      (void *)Xcs})
+        if (ptr) cudaFreeAsync(ptr, s);
+}
+
+}  // namespace ncvis_gpu

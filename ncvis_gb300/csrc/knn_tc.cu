@@ -265,14 +265,15 @@ __device__ __forceinline__ void flush_queue(float (&ls)[R], int32_t (&li)[R], fl
     __syncwarp();
 }
 
-// One query tile of work: 256 rows from row0 (rows of the matrix the tensor
-// map covers), whose candidates are rows [lo, hi) of that matrix (lo a
-// multiple of 128); row r's candidate list goes to output row r + out_off and
-// its entries c are written as c + out_off.  Without a work list a CTA takes
-// the query tiles blockIdx.x, blockIdx.x + gridDim.x, ... of one problem of N
-// rows.
+// One item of work: the query tile of 256 rows from row0 (rows at or past
+// qend are not outputs) against candidate rows [lo, hi); `cont`: the item
+// extends the previous item's query tile (no reload, lists carry over);
+// `more`: a later item extends this one (lists written after the last).
+// Without a work list a CTA takes the query tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... of one problem of N rows, each against all N.
 struct QueryTile {
-    int64_t row0, lo, hi, out_off;
+    int32_t row0, qend, lo, hi, out_off;  // N < 2^31
+    bool cont, more;
 };
 
 __device__ __forceinline__ int64_t work_items(const int64_t *__restrict__ work_begin,
@@ -282,20 +283,25 @@ __device__ __forceinline__ int64_t work_items(const int64_t *__restrict__ work_b
 }
 
 __device__ __forceinline__ QueryTile work_item(const int64_t *__restrict__ work_begin,
-                                               const int4 *__restrict__ work, int64_t it,
+                                               const TcItem *__restrict__ work, int64_t it,
                                                int64_t N) {
     QueryTile q;
     if (work_begin) {
-        const int4 w = work[work_begin[blockIdx.x] + it];
-        q.row0 = w.x;
-        q.lo = w.y;
-        q.hi = w.z;
-        q.out_off = w.w;
+        const TcItem w = work[work_begin[blockIdx.x] + it];
+        q.row0 = w.row0;
+        q.qend = w.qend;
+        q.lo = w.lo;
+        q.hi = w.hi;
+        q.out_off = w.out_off;
+        q.cont = (w.flags & kTcContinue) != 0;
+        q.more = (w.flags & kTcMore) != 0;
     } else {
-        q.row0 = ((int64_t)blockIdx.x + it * gridDim.x) * kQueryTile;
+        q.row0 = (int32_t)(((int64_t)blockIdx.x + it * gridDim.x) * kQueryTile);
+        q.qend = (int32_t)N;
         q.lo = 0;
-        q.hi = N;
+        q.hi = (int32_t)N;
         q.out_off = 0;
+        q.cont = q.more = false;
     }
     return q;
 }
@@ -305,8 +311,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     knn_select_tc(const __grid_constant__ CUtensorMap tmap,
                   const __grid_constant__ CUtensorMap tmap_c, const float *__restrict__ sqnorm,
                   int64_t N, int ksteps, int katoms, const int64_t *__restrict__ work_begin,
-                  const int4 *__restrict__ work, int32_t *__restrict__ cand_i,
-                  int *__restrict__ err) {
+                  const TcItem *__restrict__ work, const int32_t *__restrict__ row_map,
+                  int32_t *__restrict__ cand_i, int *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     SharedStorage &s = *reinterpret_cast<SharedStorage *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -355,14 +361,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint32_t a_parity = 0;
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
             const QueryTile q = work_item(work_begin, work, it, N);
-            if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1)) break;
-            mbar_expect_tx(&s.a_full, a_bytes);
-            for (int h = 0; h < 2; ++h)
-                for (int at = 0; at < katoms; ++at)
-                    tma_load_2d(s.a[h][at], &tmap, &s.a_full, at * 64, (int)(q.row0 + h * 128));
-            a_issued = true;
-            a_parity = a_phase;
-            a_phase ^= 1;
+            if (!q.cont) {
+                if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1)) break;
+                mbar_expect_tx(&s.a_full, a_bytes);
+                for (int h = 0; h < 2; ++h)
+                    for (int at = 0; at < katoms; ++at)
+                        tma_load_2d(s.a[h][at], &tmap, &s.a_full, at * 64,
+                                    (int)(q.row0 + h * 128));
+                a_issued = true;
+                a_parity = a_phase;
+                a_phase ^= 1;
+            }
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2)) break;
                 mbar_expect_tx(&s.full[stage], b_bytes);
@@ -393,8 +402,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         int acc = 0;
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
             const QueryTile q = work_item(work_begin, work, it, N);
-            if (!mbar_wait(s, &s.a_full, a_phase, err, 3)) break;
-            a_phase ^= 1;
+            if (!q.cont) {
+                if (!mbar_wait(s, &s.a_full, a_phase, err, 3)) break;
+                a_phase ^= 1;
+            }
             tmem_fence_after();
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.acc_empty[acc], acc_phase ^ 1, err, 4)) break;
@@ -416,7 +427,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 acc ^= 1;
                 if (acc == 0) acc_phase ^= 1;
             }
-            umma_commit(&s.a_empty);
+            if (!q.more) umma_commit(&s.a_empty);
         }
         // Every issued MMA completes before TMEM is released.
         umma_commit(&s.drain);
@@ -434,19 +445,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         constexpr int kC = R <= 32 ? 32 : 16;
         uint32_t acc_phase = 0;
         int acc = 0;
+        float ls[R];
+        int32_t li[R];
+        float worst = FLT_MAX;
+        int qlen = 0;
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
             const QueryTile q = work_item(work_begin, work, it, N);
             const int64_t grow = q.row0 + row_in_tile;
-            const bool live = grow < q.hi;
-            float ls[R];
-            int32_t li[R];
+            const bool live = grow < q.qend;
+            if (!q.cont) {
 #pragma unroll
-            for (int t = 0; t < R; ++t) {
-                ls[t] = FLT_MAX;
-                li[t] = -1;
+                for (int t = 0; t < R; ++t) {
+                    ls[t] = FLT_MAX;
+                    li[t] = -1;
+                }
+                worst = FLT_MAX;
+                qlen = 0;
             }
-            float worst = FLT_MAX;
-            int qlen = 0;
             bool ok = true;
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
                 if (!mbar_wait(s, &s.acc_full[acc], acc_phase, err, 6)) {
@@ -455,7 +470,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 tmem_fence_after();
                 const int64_t c0 = ct * kCandTile;
-                const bool tail = c0 + kCandTile > q.hi;
+                // A tile reaching outside [lo, hi): its outside columns are masked.
+                const bool tail = c0 < q.lo || c0 + kCandTile > q.hi;
 #pragma unroll 1
                 for (int chunk = 0; chunk < kCandTile / kC; ++chunk) {
                     float v[kC];
@@ -469,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if constexpr (!kIP) {
                         // The chunk's candidate norms, the same for every lane:
                         // 16-byte loads where the chunk lies inside the rows.
-                        if (cb + kC <= q.hi) {
+                        if (cb >= q.lo && cb + kC <= q.hi) {
 #pragma unroll
                             for (int j = 0; j < kC; j += 4) {
                                 const float4 nc =
@@ -483,7 +499,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                             for (int j = 0; j < kC; ++j) {
                                 const int64_t c = cb + j;
-                                const float nc = (c < q.hi) ? __ldg(sqnorm + c) : 0.f;
+                                const float nc =
+                                    (c >= q.lo && c < q.hi) ? __ldg(sqnorm + c) : 0.f;
                                 v[j] = fmaf(-2.f, v[j], nc);
                             }
                         }
@@ -491,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (tail) {
 #pragma unroll
                         for (int j = 0; j < kC; ++j)
-                            if (cb + j >= q.hi) v[j] = kIP ? -FLT_MAX : FLT_MAX;
+                            if (cb + j < q.lo || cb + j >= q.hi) v[j] = kIP ? -FLT_MAX : FLT_MAX;
                     }
                     // Best score of each 8-column group, then of the chunk.
                     constexpr int kG = kC / 8;
@@ -546,12 +563,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                     flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
             }
             if (!ok) break;
+            if (q.more) continue;  // the next item extends this query tile
             flush_queue<R>(ls, li, worst, qlen, s.queue_v, s.queue_i, etid);
             if (live) {
+                const int64_t orow = row_map ? (int64_t)row_map[grow] : grow + q.out_off;
 #pragma unroll
                 for (int t = 0; t < R; ++t)
-                    cand_i[(grow + q.out_off) * R + t] =
-                        li[t] >= 0 ? (int32_t)(li[t] + q.out_off) : -1;
+                    cand_i[orow * R + t] =
+                        li[t] < 0 ? -1
+                                  : (row_map ? row_map[li[t]] : (int32_t)(li[t] + q.out_off));
             }
         }
     }
@@ -597,53 +617,88 @@ KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor, int dist) {
 bool knn_tc_supported(int D, int R) { return D >= 1 && D <= 64 * kMaxAtoms && (R == 32 || R == 64); }
 
 
-void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
-                          const KnnTcPlan &plan, int dist, int32_t *cand_i, float * /*cand_d*/,
-                          int *timeout_flag, cudaStream_t s, const TcWork *work,
-                          const __nv_bfloat16 *Xc) {
-    require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
+namespace {
+
+void encode_rows(const __nv_bfloat16 *base, int64_t rows, int ldb, CUtensorMap &map) {
+    cuuint64_t dims[2] = {(cuuint64_t)ldb, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ldb * 2};
+    cuuint32_t box[2] = {64, 128};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base,
+                                      dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    require(r == CUDA_SUCCESS,
+            "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")", kCudaError);
+}
+
+void launch_select(const CUtensorMap &map, const CUtensorMap &map_c, const float *sqnorm,
+                   int64_t N, const KnnTcPlan &plan, bool ip, int32_t *cand_i, int *timeout_flag,
+                   cudaStream_t s, const TcWork *work) {
     const int ksteps = (plan.ldb + 15) / 16;
     const int katoms = (ksteps * 16 + 63) / 64;
-    require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
-    require(((uintptr_t)Xb & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
-    require(((uintptr_t)sqnorm & 15) == 0, "knn: squared norms must be 16-byte aligned");
-    require(!plan.fold || (Xc && ((uintptr_t)Xc & 15) == 0),
-            "knn: the folded squared-L2 mode needs a 16-byte aligned candidate copy");
-    auto encode = [&](const __nv_bfloat16 *base, CUtensorMap &map) {
-        cuuint64_t dims[2] = {(cuuint64_t)plan.ldb, (cuuint64_t)N};
-        cuuint64_t strides[1] = {(cuuint64_t)plan.ldb * 2};
-        cuuint32_t box[2] = {64, 128};
-        cuuint32_t estr[2] = {1, 1};
-        CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base,
-                                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                          CU_TENSOR_MAP_SWIZZLE_128B,
-                                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        require(r == CUDA_SUCCESS,
-                "knn: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")", kCudaError);
-    };
-    // Queries come from Xb, candidates from Xc in the folded mode (else Xb).
-    CUtensorMap map, map_c;
-    encode(Xb, map);
-    encode(plan.fold ? Xc : Xb, map_c);
     const size_t smem = sizeof(SharedStorage) + 1024;
     const int64_t n_qt = (N + kQueryTile - 1) / kQueryTile;
     const unsigned grid =
         work ? (unsigned)work->ctas : (unsigned)std::min<int64_t>(n_qt, num_sms());
-    // The folded squared-L2 product <q, c> - |c|^2 / 2 ranks like an inner product.
-    const bool ip = dist != kSquaredL2 || plan.fold;
     const int64_t *work_begin = work ? work->begin : nullptr;
-    const int4 *items = work ? work->items : nullptr;
+    const TcItem *items = work ? work->items : nullptr;
+    const int32_t *row_map = work ? work->map : nullptr;
+    if (grid == 0) return;
     auto go = [&](auto kernel) {
         NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
         NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, map_c, sqnorm, N, ksteps, katoms,
-                     work_begin, items, cand_i, timeout_flag);
+                     work_begin, items, row_map, cand_i, timeout_flag);
     };
     if (plan.R == 32)
         ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);
     else
         ip ? go(knn_select_tc<64, true>) : go(knn_select_tc<64, false>);
+}
+
+void check_plan(const KnnTcPlan &plan) {
+    const int ksteps = (plan.ldb + 15) / 16;
+    const int katoms = (ksteps * 16 + 63) / 64;
+    require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
+    require(plan.R == 32 || plan.R == 64, "knn: the tensor-core kernel keeps 32 or 64 candidates");
+}
+
+}  // namespace
+
+void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
+                          const KnnTcPlan &plan, int dist, int32_t *cand_i, float * /*cand_d*/,
+                          int *timeout_flag, cudaStream_t s, const TcWork *work,
+                          const __nv_bfloat16 *Xc) {
+    require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
+    check_plan(plan);
+    require(((uintptr_t)Xb & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
+    require(((uintptr_t)sqnorm & 15) == 0, "knn: squared norms must be 16-byte aligned");
+    require(!plan.fold || (Xc && ((uintptr_t)Xc & 15) == 0),
+            "knn: the folded squared-L2 mode needs a 16-byte aligned candidate copy");
+    // Queries come from Xb, candidates from Xc in the folded mode (else Xb).
+    CUtensorMap map, map_c;
+    encode_rows(Xb, N, plan.ldb, map);
+    encode_rows(plan.fold ? Xc : Xb, N, plan.ldb, map_c);
+    // The folded squared-L2 product <q, c> - |c|^2 / 2 ranks like an inner product.
+    const bool ip = dist != kSquaredL2 || plan.fold;
+    launch_select(map, map_c, sqnorm, N, plan, ip, cand_i, timeout_flag, s, work);
+}
+
+void launch_knn_select_tc_pair(const __nv_bfloat16 *Q, int64_t nq, const __nv_bfloat16 *Cm,
+                               int64_t nc, const float *c_sqnorm, const KnnTcPlan &plan, bool ip,
+                               int32_t *cand_i, int *timeout_flag, cudaStream_t s,
+                               const TcWork &work) {
+    require(nq < (int64_t(1) << 31) && nc < (int64_t(1) << 31), "knn: rows must be below 2^31");
+    check_plan(plan);
+    require((((uintptr_t)Q | (uintptr_t)Cm) & 15) == 0, "knn: BF16 rows must be 16-byte aligned");
+    require(ip || (c_sqnorm && ((uintptr_t)c_sqnorm & 15) == 0),
+            "knn: squared L2 without folded norms needs 16-byte aligned candidate norms");
+    CUtensorMap map, map_c;
+    encode_rows(Q, nq, plan.ldb, map);
+    encode_rows(Cm, nc, plan.ldb, map_c);
+    launch_select(map, map_c, c_sqnorm, nq, plan, ip, cand_i, timeout_flag, s, &work);
 }
 
 }  // namespace ncvis_gpu

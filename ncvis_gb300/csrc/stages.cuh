@@ -57,19 +57,51 @@ struct KnnTcPlan {
 };
 KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor, int dist);
 bool knn_tc_supported(int D, int R);
-// Query tiles of several problems for one launch (device arrays): CTA b takes
-// items[begin[b] .. begin[b + 1]), each {row0, lo, hi, out_off} (int32): 256
-// query rows from row0, candidates rows [lo, hi) of Xb (lo a multiple of 256),
-// outputs at row + out_off with entries c + out_off.
+// One item of a tensor-core launch's work list: the 256 query rows from row0
+// (rows at or past qend are not outputs) against candidate rows [lo, hi).
+// Outputs go to row + out_off with entries c + out_off, or, when the work has
+// a row map, to map[row] with entries map[c].  kTcContinue: the item extends
+// the previous item's query tile (same row0: the tile is not reloaded and its
+// lists carry over); kTcMore: a later item continues this one (the lists are
+// written after the last item of a query tile).
+constexpr int kTcContinue = 1;
+constexpr int kTcMore = 2;
+struct alignas(16) TcItem {
+    int32_t row0, qend, lo, hi;
+    int32_t out_off, flags, pad0, pad1;
+};
+// Work of one launch (device arrays): CTA b takes items[begin[b] .. begin[b+1]).
 struct TcWork {
     int ctas;
     const int64_t *begin;
-    const int4 *items;
+    const TcItem *items;
+    const int32_t *map;  // optional row map (sorted row -> output row), or null
 };
 void launch_knn_select_tc(const __nv_bfloat16 *Xb, const float *sqnorm, int64_t N,
                           const KnnTcPlan &plan, int dist, int32_t *cand_i, float *cand_d,
                           int *timeout_flag, cudaStream_t s, const TcWork *work = nullptr,
                           const __nv_bfloat16 *Xc = nullptr);
+// Approximate candidate selection (inverted file): C cells from k-means on
+// the BF16 rows, each cell searched against its `probe` nearest cells.
+struct IvfPlan {
+    int C = 1, probe = 1, iters = 4;
+};
+IvfPlan plan_ivf(int64_t N, int lists, int probe);
+// Xp: preprocessed FP32 rows; Xb (and Xc with the folded squared-L2 product)
+// as for launch_knn_select_tc; cand_i [N, tp.R] receives the candidates in
+// original numbering (its first N * 32 entries also serve as scratch).
+void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc, int64_t N,
+                 int D, const KnnTcPlan &tp, int dist, const IvfPlan &ip, uint64_t seed,
+                 int32_t *cand_i, int *timeout_flag, cudaStream_t s);
+
+// Queries from Q (nq rows) against candidates from Cm (nc rows), both bf16
+// [rows, plan.ldb]; c_sqnorm: candidate squared norms (used for squared L2
+// without the folded norms); `ip`: rank by the product (inner-product spaces,
+// or squared L2 with the folded candidate copy).  A work list is required.
+void launch_knn_select_tc_pair(const __nv_bfloat16 *Q, int64_t nq, const __nv_bfloat16 *Cm,
+                               int64_t nc, const float *c_sqnorm, const KnnTcPlan &plan, bool ip,
+                               int32_t *cand_i, int *timeout_flag, cudaStream_t s,
+                               const TcWork &work);
 
 // ---- K5 symmetrize (src/knntable.cpp:24-99, src/ncvis.cpp:155-173) -----------
 size_t symmetrize_workspace_bytes(int64_t N, int k);

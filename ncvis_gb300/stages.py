@@ -49,6 +49,22 @@ def knn(X, k: int, distance: int = 0, precision: int = _lib.KNN_FP32, rerank_fac
     return inds, dists
 
 
+def knn_ivf(X, k: int, distance: int = 0, lists: int = 0, probe: int = 0,
+            rerank_factor: int = 0):
+    """Approximate kNN table (inverted file: k-means cells on BF16 rows,
+    each cell searched against its `probe` nearest cells on the tensor cores,
+    exact FP32 rerank); the row contract of `knn`."""
+    torch = _torch()
+    X = _f32(X)
+    N, D = X.shape
+    inds = torch.empty((N, k), dtype=torch.int32, device=X.device)
+    dists = torch.empty((N, k), dtype=torch.float32, device=X.device)
+    _lib.check(_lib.lib().ncvis_knn_ivf_device(X.data_ptr(), N, D, distance, k, rerank_factor,
+                                               lists, probe, inds.data_ptr(), dists.data_ptr(),
+                                               _stream()))
+    return inds, dists
+
+
 def symmetrize(inds, dists):
     """Bit-exact symmetrized CSR of a kNN table: (row_ptr int64 [N+1],
     cols int32 [E], vals float32 [E], src int32 [E])."""
