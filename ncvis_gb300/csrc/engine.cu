@@ -546,6 +546,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     const size_t o_ti = L.take(sizeof(int64_t) * (B + 1));
     const size_t o_eoff = L.take(sizeof(int64_t) * (B + 1));
     const size_t o_cp = L.take(sizeof(int64_t) * (B + 1));
+    const size_t o_bp = L.take(sizeof(int64_t) * (B + 1));
     const size_t o_seed = L.take(sizeof(uint64_t) * B);
     const size_t o_Qs = L.take(sizeof(float) * B);
     const size_t o_cq = L.take(sizeof(float) * max_chains);
@@ -575,6 +576,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     int64_t *d_off = (int64_t *)(base + o_off), *d_tq = (int64_t *)(base + o_tq);
     int64_t *d_ti = (int64_t *)(base + o_ti), *d_eoff = (int64_t *)(base + o_eoff);
     int64_t *d_cp = (int64_t *)(base + o_cp);
+    int64_t *d_bp = (int64_t *)(base + o_bp);
     uint64_t *d_seed = (uint64_t *)(base + o_seed);
     float *Qs = (float *)(base + o_Qs), *chain_q = (float *)(base + o_cq);
     float *Ytune = (float *)(base + o_Yt), *Qtune = (float *)(base + o_Qt);
@@ -683,25 +685,44 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     g.b = p.b;
     g.alpha = p.alpha;
     g.alpha_Q = p.alpha_Q;
-    std::vector<int64_t> h_cp;
+    std::vector<int64_t> h_cp, h_bp;
+    // Noise staged in shared memory (d <= 4, the default Hogwild mode): every
+    // block of chains within one problem.
+    const bool staged = d <= 4 && o.sgd_mode == NCVIS_SGD_HOGWILD;
+    int64_t n_blocks = 0;
+    auto set_layout = [&](int edges_per_chain) {
+        g.n_chains = chain_layout(edges_per_chain, h_cp);
+        const int64_t T = sgd_window_batched_threads();
+        h_bp.assign(B + 1, 0);
+        for (size_t q = 0; q < B; ++q) h_bp[q + 1] = h_bp[q] + (h_cp[q + 1] - h_cp[q] + T - 1) / T;
+        n_blocks = h_bp[B];
+        NCVIS_CUDA(cudaMemcpyAsync(d_cp, h_cp.data(), sizeof(int64_t) * (B + 1),
+                                   cudaMemcpyHostToDevice, s));
+        NCVIS_CUDA(cudaMemcpyAsync(d_bp, h_bp.data(), sizeof(int64_t) * (B + 1),
+                                   cudaMemcpyHostToDevice, s));
+    };
+    auto run_epochs = [&](const SgdBatch &t, const size_t *plan, cudaStream_t st) {
+        if (staged)
+            run_sgd_window_batched(t, d_bp, n_blocks, plan, st);
+        else
+            run_sgd_hogwild_batched(t, plan, st);
+    };
     if (p.n_epochs > 0 && E > 0) {
         // Autotune edges per chain on a scratch copy of the embedding (one epoch each).
-        const std::string key = "sgd_batched d=" + std::to_string(d) + " B=" + std::to_string(B) +
+        const std::string key = std::string(staged ? "sgd_batched_staged" : "sgd_batched") +
+                                " d=" + std::to_string(d) + " B=" + std::to_string(B) +
                                 " E~2^" + std::to_string((int)std::log2((double)std::max<int64_t>(E, 1)));
         const int chosen = tuner.pick(key, {16, 32, 64, 128}, [&](int epc) {
-            g.n_chains = chain_layout(epc, h_cp);
-            NCVIS_CUDA(cudaMemcpyAsync(d_cp, h_cp.data(), sizeof(int64_t) * (B + 1),
-                                       cudaMemcpyHostToDevice, s));
+            set_layout(epc);
             NCVIS_CUDA(cudaMemcpyAsync(Ytune, dY, sizeof(float) * total * d, cudaMemcpyDeviceToDevice, s));
             NCVIS_CUDA(cudaMemsetAsync(Qtune, 0, sizeof(float) * B, s));
             SgdBatch t = g;
             t.Y = Ytune;
             t.Qs = Qtune;
             t.n_epochs = 1;
-            run_sgd_hogwild_batched(t, noise.data() + (p.n_epochs - 1), s);
+            run_epochs(t, noise.data() + (p.n_epochs - 1), s);
         }, s);
-        g.n_chains = chain_layout(chosen, h_cp);
-        NCVIS_CUDA(cudaMemcpyAsync(d_cp, h_cp.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
+        set_layout(chosen);
         NCVIS_CUDA(cudaMemsetAsync(Qs, 0, sizeof(float) * B, s));
         g.Y = dY;
         g.Qs = Qs;
@@ -713,7 +734,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         cudaGraphExec_t exec = nullptr;
         NCVIS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         try {
-            run_sgd_hogwild_batched(g, noise.data(), cs);
+            run_epochs(g, noise.data(), cs);
         } catch (...) {
             cudaStreamEndCapture(cs, &graph);
             if (graph) cudaGraphDestroy(graph);

@@ -432,13 +432,27 @@ __device__ __forceinline__ uint32_t segment_start(uint32_t k0, uint32_t k1, uint
     return bounded_index(x.v[0], x.v[1], N);
 }
 
+// A block's window: W rows of the problem of N rows starting at row `base`
+// of Y, either 256-row segments at the starts in `seg` (wrapping at N) or,
+// `whole`, the problem's rows in order (W == N).
+struct WindowSpec {
+    const uint32_t *seg;
+    uint32_t W, N, base;
+    bool whole;
+};
+
+__device__ __forceinline__ uint32_t spec_row(const WindowSpec &w, uint32_t u) {
+    return w.base + (w.whole ? u : window_row(w.seg, u, w.N));
+}
+
 // A noise sample whose window row is the edge source i is redrawn from
 // blocks (e_lo, e_hi ^ retry<<16, tag, s/2 | 3<<30) under key (k0 ^ retry, k1),
 // up to 64 times; then the next window row is taken.
 __device__ __forceinline__ uint32_t window_redraw(uint32_t k0, uint32_t k1, uint64_t e, uint32_t tag,
                                                   uint32_t s, uint32_t u, uint32_t i,
-                                                  const uint32_t *seg, uint32_t W, uint32_t N) {
-    for (uint32_t retry = 1; window_row(seg, u, N) == i; ++retry) {
+                                                  const WindowSpec &ws) {
+    const uint32_t W = ws.W;
+    for (uint32_t retry = 1; spec_row(ws, u) == i; ++retry) {
         if (retry > 64) {
             u = (u + 1 == W) ? 0 : u + 1;
             break;
@@ -517,7 +531,7 @@ __device__ __forceinline__ void window_sample(float *win, uint32_t u, Vec<D> &yi
 __device__ __forceinline__ void load_group(const int32_t *__restrict__ src,
                                            const int32_t *__restrict__ dst, int64_t e, int64_t b,
                                            int32_t (&sv)[4], int32_t (&dv)[4]) {
-    if (e + 4 <= b) {
+    if (e + 4 <= b && (e & 3) == 0) {
         const int4 s4 = __ldg(reinterpret_cast<const int4 *>(src + e));
         const int4 d4 = __ldg(reinterpret_cast<const int4 *>(dst + e));
         sv[0] = s4.x, sv[1] = s4.y, sv[2] = s4.z, sv[3] = s4.w;
@@ -547,13 +561,13 @@ __device__ __forceinline__ void gather_group(const float *Y, const int32_t (&sv)
 // gathered row that this chain wrote in between (an earlier positive row or
 // a stored source of the group) is read again, so the chain always sees its
 // own updates.
-template <int D>
+template <int D, bool kWhole>
 __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict__ src,
                                              const int32_t *__restrict__ dst, int64_t a, int64_t b,
-                                             uint32_t N, const EpochConst &k, float &Qc,
-                                             uint32_t key0, uint32_t key1, uint32_t tag,
-                                             float *win, const uint32_t *seg, uint32_t W,
-                                             bool &have, uint32_t &ci, Vec<D> &yi) {
+                                             const EpochConst &k, float &Qc, uint32_t key0,
+                                             uint32_t key1, uint32_t tag, float *win,
+                                             const WindowSpec &ws, bool &have, uint32_t &ci,
+                                             Vec<D> &yi) {
     for (int64_t e = a; e < b; e += 4) {
         int32_t sv[4], dv[4];
         load_group(src, dst, e, b, sv, dv);
@@ -593,16 +607,34 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
                     yi.v[c] = (yi.v[c] + dx) - dx;
                 }
             }
-            for (int s0 = 0; s0 < k.nu; s0 += 8) {
-                const Philox4x32 r = window_block(key0, key1, (uint64_t)(e + q), tag,
-                                                  (uint32_t)(s0 >> 3));
+            if constexpr (kWhole) {
+                // Whole-problem window of any size: the four 32-bit words of a
+                // Philox block give four picks by multiply-shift.
+                for (int s0 = 0; s0 < k.nu; s0 += 4) {
+                    const Philox4x32 r = philox4x32_10((uint32_t)(e + q), (uint32_t)((e + q) >> 32),
+                                                       tag, (uint32_t)(s0 >> 2) | 0x50000000u,
+                                                       key0, key1);
 #pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    if (s0 + t >= k.nu) break;
-                    const uint32_t u = window_redraw(key0, key1, (uint64_t)(e + q), tag,
-                                                     (uint32_t)(s0 + t), window_pick(r, t, W), i,
-                                                     seg, W, N);
-                    window_sample<D>(win, u, yi, k, Qc);
+                    for (int t = 0; t < 4; ++t) {
+                        if (s0 + t >= k.nu) break;
+                        const uint32_t pick = (uint32_t)(((uint64_t)r.v[t] * ws.W) >> 32);
+                        const uint32_t u = window_redraw(key0, key1, (uint64_t)(e + q), tag,
+                                                         (uint32_t)(s0 + t), pick, i, ws);
+                        window_sample<D>(win, u, yi, k, Qc);
+                    }
+                }
+            } else {
+                for (int s0 = 0; s0 < k.nu; s0 += 8) {
+                    const Philox4x32 r = window_block(key0, key1, (uint64_t)(e + q), tag,
+                                                      (uint32_t)(s0 >> 3));
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        if (s0 + t >= k.nu) break;
+                        const uint32_t u = window_redraw(key0, key1, (uint64_t)(e + q), tag,
+                                                         (uint32_t)(s0 + t),
+                                                         window_pick(r, t, ws.W), i, ws);
+                        window_sample<D>(win, u, yi, k, Qc);
+                    }
                 }
             }
         }
@@ -642,8 +674,9 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
         __syncthreads();
         const int64_t a = min(e1, e0 + (int64_t)r * round_edges);
         const int64_t b = min(e1, a + round_edges);
-        window_edges<D>(Y, src, dst, a, b, N, k, Qc, key0, key1, (uint32_t)epoch, win, seg,
-                                 W, have, ci, yi);
+        const WindowSpec ws{seg, W, N, 0u, false};
+        window_edges<D, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
+                               have, ci, yi);
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < W; u += kWinThreads) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
@@ -670,6 +703,81 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
         for (int w = 0; w < kWinThreads / 32; ++w) t += red[w];
         q_part[blockIdx.x] = t;
     }
+}
+
+// Batched problems with staged noise: every block's chains belong to one
+// problem (problem p owns blocks [bp[p], bp[p+1]) and chains [cp[p], cp[p+1]),
+// the last block of a problem partly idle); the window is the problem's rows
+// when they fit (exact uniform picks over them) or 256-row segments at uniform
+// starts within the problem otherwise.
+constexpr int kBatThreads = 128;
+constexpr uint32_t kBatWindow = 1024;  // rows; two copies of d <= 4 floats fit 32 KB
+
+template <int D>
+__global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
+    float *__restrict__ Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
+    const int64_t *__restrict__ off, const int64_t *__restrict__ eoff,
+    const int64_t *__restrict__ cp, const int64_t *__restrict__ bp, int B,
+    const float *__restrict__ Qs, float *__restrict__ chain_q, EpochConst k, int epoch,
+    uint32_t key0, uint32_t key1, int round_edges) {
+    __shared__ __align__(16) float win[kBatWindow * D];
+    __shared__ __align__(16) float loaded[kBatWindow * D];
+    __shared__ uint32_t seg[kBatWindow / kSegRows];
+    const int p = segment_of(bp, B, (int64_t)blockIdx.x);
+    const int64_t lc = ((int64_t)blockIdx.x - bp[p]) * kBatThreads + threadIdx.x;
+    const int64_t nc = cp[p + 1] - cp[p];
+    const int64_t Ep = eoff[p + 1] - eoff[p];
+    const int64_t chunk = ((Ep + nc - 1) / nc + 3) & ~(int64_t)3;
+    const bool active = lc < nc;
+    const int64_t e0 = eoff[p] + (active ? min(Ep, lc * chunk) : Ep);
+    const int64_t e1 = eoff[p] + (active ? min(Ep, (lc + 1) * chunk) : Ep);
+    const uint32_t base = (uint32_t)off[p];
+    const uint32_t Np = (uint32_t)(off[p + 1] - off[p]);
+    const bool whole = Np <= kBatWindow;
+    const uint32_t W = whole ? Np : kBatWindow;
+    const int rounds = (int)((chunk + round_edges - 1) / round_edges);
+    const WindowSpec ws{seg, W, Np, base, whole};
+    float Qc = Qs[p];
+    bool have = false;
+    uint32_t ci = 0;
+    Vec<D> yi;
+#pragma unroll
+    for (int c = 0; c < D; ++c) yi.v[c] = 0.f;
+    for (int r = 0; r < rounds; ++r) {
+        if (!whole)
+            for (uint32_t t = threadIdx.x; t < W / kSegRows; t += kBatThreads)
+                seg[t] = segment_start(key0, key1, blockIdx.x, (uint32_t)r, (uint32_t)epoch, t, Np);
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < W; u += kBatThreads) {
+            const Vec<D> v = load_row<D>(Y, spec_row(ws, u));
+            store_win<D>(win, u, v);
+            store_win<D>(loaded, u, v);
+        }
+        __syncthreads();
+        const int64_t a = min(e1, e0 + (int64_t)r * round_edges);
+        const int64_t b = min(e1, a + round_edges);
+        if (whole)
+            window_edges<D, true>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
+                                  have, ci, yi);
+        else
+            window_edges<D, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
+                                   have, ci, yi);
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < W; u += kBatThreads) {
+            const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
+            Vec<D> minus;
+            bool moved = false;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                minus.v[c] = was.v[c] - now.v[c];
+                moved |= (minus.v[c] != 0.f);
+            }
+            if (moved) sub_row<D>(Y, spec_row(ws, u), minus);
+        }
+        __syncthreads();
+    }
+    if (have) store_row<D>(Y, ci, yi);
+    if (active) chain_q[cp[p] + lc] = Qc;
 }
 
 // ---------------------------------------------------------------- replay
@@ -939,6 +1047,43 @@ void run_sgd_window(const SgdArgs &g, int epoch_begin, int epoch_end, const size
                                                    chunk, total_chains, W, round_edges);
         }
         NCVIS_LAUNCH(reduce_q, 1, 1024, 0, s, q_part, (int)blocks, total_chains, g.Q);
+    }
+}
+
+int sgd_window_batched_threads() { return kBatThreads; }
+
+void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks,
+                            const size_t *n_noise, cudaStream_t s) {
+    require(g.d >= 1 && g.d <= 4, "batched optimize: d must be in [1, 4]");
+    uint32_t key0, key1;
+    noise_key(g.seed, key0, key1);
+    const int round_edges = 16;
+    for (int ep = 0; ep < g.n_epochs; ++ep) {
+        SgdArgs one{0, g.d, 0, nullptr, nullptr, nullptr, nullptr, g.seed, g.n_epochs,
+                    g.a, g.b, g.alpha, g.alpha_Q};
+        EpochConst k = epoch_const(one, ep, (int)n_noise[ep]);
+        switch (g.d) {
+            case 1:
+                NCVIS_LAUNCH(sgd_epoch_window_batched<1>, (unsigned)n_blocks, kBatThreads, 0, s,
+                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
+                             ep, key0, key1, round_edges);
+                break;
+            case 2:
+                NCVIS_LAUNCH(sgd_epoch_window_batched<2>, (unsigned)n_blocks, kBatThreads, 0, s,
+                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
+                             ep, key0, key1, round_edges);
+                break;
+            case 3:
+                NCVIS_LAUNCH(sgd_epoch_window_batched<3>, (unsigned)n_blocks, kBatThreads, 0, s,
+                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
+                             ep, key0, key1, round_edges);
+                break;
+            default:
+                NCVIS_LAUNCH(sgd_epoch_window_batched<4>, (unsigned)n_blocks, kBatThreads, 0, s,
+                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
+                             ep, key0, key1, round_edges);
+        }
+        NCVIS_LAUNCH(reduce_q_batched, g.B, 256, 0, s, g.chain_q, g.cp, g.Qs);
     }
 }
 
