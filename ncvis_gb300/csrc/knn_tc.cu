@@ -10,6 +10,7 @@
 //   * warp 0 issues TMA; warps 1 and 10 issue tcgen05.mma (M=128, N=128,
 //     K=16 steps), one query half each, into one of two double-buffered
 //     2x128-column FP32 accumulators (512 TMEM columns; warp 1 allocates);
+//     each half hands its accumulators to its own four epilogue warps;
 //   * warps 2..9 own one query row each (TMEM lane = row; warp % 4 selects
 //     the lane quadrant): they read the accumulator with tcgen05.ld in
 //     32-column chunks, turn dot products into ranking scores (-<q,c> for the
@@ -64,7 +65,7 @@ struct SharedStorage {
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t a_full, a_empty;
-    uint64_t acc_full[2], acc_empty[2];
+    uint64_t acc_full[2][2], acc_empty[2][2];  // [buffer][query half]
     uint64_t drain;
     uint32_t tmem_base;
     volatile int abort;
@@ -330,10 +331,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         mbar_init(&s.a_full, 1);
         mbar_init(&s.a_empty, 2);
-        for (int i = 0; i < 2; ++i) {
-            mbar_init(&s.acc_full[i], 2);
-            mbar_init(&s.acc_empty[i], kEpiWarps);
-        }
+        // Each query half has its own accumulator hand-off: its MMA warp and
+        // its four epilogue warps, so one half's slow tile does not hold the other.
+        for (int i = 0; i < 2; ++i)
+            for (int hh = 0; hh < 2; ++hh) {
+                mbar_init(&s.acc_full[i][hh], 1);
+                mbar_init(&s.acc_empty[i][hh], kEpiWarps / 2);
+            }
         mbar_init(&s.drain, 2);
         s.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             tmem_fence_after();
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
-                if (!mbar_wait(s, &s.acc_empty[acc], acc_phase ^ 1, err, 4)) break;
+                if (!mbar_wait(s, &s.acc_empty[acc][h], acc_phase ^ 1, err, 4)) break;
                 if (!mbar_wait(s, &s.full[stage], phase, err, 5)) break;
                 tmem_fence_after();
                 {
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
                 umma_commit(&s.empty[stage]);
-                umma_commit(&s.acc_full[acc]);
+                umma_commit(&s.acc_full[acc][h]);
                 if (++stage == kStages) stage = 0, phase ^= 1;
                 acc ^= 1;
                 if (acc == 0) acc_phase ^= 1;
@@ -464,7 +468,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             bool ok = true;
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
-                if (!mbar_wait(s, &s.acc_full[acc], acc_phase, err, 6)) {
+                if (!mbar_wait(s, &s.acc_full[acc][h], acc_phase, err, 6)) {
                     ok = false;
                     break;
                 }
@@ -552,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 tmem_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&s.acc_empty[acc]);
+                if (lane == 0) mbar_arrive(&s.acc_empty[acc][h]);
                 acc ^= 1;
                 if (acc == 0) acc_phase ^= 1;
                 // Queues past half full are flushed here, after the accumulator
