@@ -36,7 +36,7 @@ N_FULL, D_FULL, K_NN, D_EMB, EPOCHS, INIT_EPOCHS = 1_024_000, 100, 15, 2, 50, 20
 SAMPLE_N = 65_536  # CPU-baseline sample of the same generator
 # DRAM bytes (read + write) of one full-size BF16 kNN-selection launch, from the
 # ncu capture in profiles/knn_select_tc_1024000x100_dram.md.
-KNN_TRAFFIC_BYTES = 9.71e9
+KNN_TRAFFIC_BYTES = 9.60e9
 
 
 def parse():
