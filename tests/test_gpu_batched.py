@@ -87,3 +87,19 @@ def test_batched_rejects_bad_layout(cuda):
     vis = ncvis.NCVis()
     with pytest.raises(ncvis.NcvisError, match="at least two points"):
         vis.fit_transform_batched([np.zeros((1, 3), np.float32), np.ones((5, 3), np.float32)])
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 4])
+def test_batched_tiny_and_boundary_problems(cuda, d):
+    """Problems of 2 and 3 points, one just below and one just above the
+    1,024-row shared-memory window of the staged optimizer (the whole problem
+    staged, or segments of it), in every embedding width the staged kernel
+    has: all finite, each problem's rows in place."""
+    import ncvis_gb300 as ncvis
+    sizes = [2, 3, 1024, 1025, 17]
+    Xs = _problems(sizes, D=8, seed=40 + d)
+    Ys = ncvis.NCVis(d=d, random_seed=3).fit_transform_batched(Xs, seeds=[1, 2, 3, 4, 5])
+    assert [Y.shape for Y in Ys] == [(n, d) for n in sizes]
+    for Y in Ys:
+        assert np.isfinite(Y).all()
+        assert np.abs(Y).max() > 0

@@ -148,3 +148,15 @@ def test_rejects_unfolded_squared_l2(cuda):
     X = np.random.default_rng(3).normal(size=(600, 127)).astype(np.float32)
     with pytest.raises(_lib.NcvisError, match="ivf"):
         _ivf(cuda, X, 5, 0)
+
+
+@pytest.mark.parametrize("N", [2, 5, 40, 300])
+def test_tiny_inputs_equal_exact(cuda, N):
+    """Tiny inputs: one or a few cells; every cell probed by default, so the
+    rows equal the exact BF16 search's."""
+    X = np.random.default_rng(N).normal(size=(N, 12)).astype(np.float32)
+    k = min(15, N - 1)
+    gi, gd = _ivf(cuda, X, k, 2)
+    ei, ed = _exact_bf16(cuda, X, k, 2)
+    assert all(np.array_equal(np.sort(a), np.sort(b)) for a, b in zip(gi, ei))
+    assert np.allclose(gd, ed, rtol=1e-6, atol=1e-6)
