@@ -75,9 +75,46 @@ __global__ void __launch_bounds__(kThreads) spmm_rows(int64_t N, int d,
     block_partial(sums, d, part);
 }
 
-// spmm_rows for d <= 4: the column indices and rows of eight edges are
-// loaded together before they are added in CSR order (the same sums, one
-// memory round trip per eight edges instead of two per edge).
+// Row i's alpha-weighted neighbour sum for d <= 4: the column indices and
+// rows of eight edges are loaded together before they are added in CSR order
+// (the same sums as one edge at a time, one memory round trip per eight edges
+// instead of two per edge).
+template <int D>
+__device__ __forceinline__ void row_average(const int64_t *__restrict__ row_ptr,
+                                            const int32_t *__restrict__ cols, float alpha,
+                                            const float *__restrict__ Yold, int64_t i,
+                                            float (&acc)[D]) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = 0.f;
+    const int64_t p0 = row_ptr[i], p1 = row_ptr[i + 1];
+    for (int64_t p = p0; p < p1; p += 8) {
+        int32_t cc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cc[k] = (p + k < p1) ? __ldg(cols + p + k) : -1;
+        float yv[8][D];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (cc[k] >= 0) {
+                if constexpr (D == 2) {
+                    const float2 t = __ldg(reinterpret_cast<const float2 *>(Yold) + cc[k]);
+                    yv[k][0] = t.x;
+                    yv[k][1] = t.y;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) yv[k][c] = __ldg(Yold + (int64_t)cc[k] * D + c);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (cc[k] >= 0) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) acc[c] = __fadd_rn(acc[c], __fmul_rn(alpha, yv[k][c]));
+            }
+    }
+}
+
+// spmm_rows for d <= 4 (row_average per row).
 template <int D>
 __global__ void __launch_bounds__(kThreads) spmm_rows_d(int64_t N, const int64_t *__restrict__ row_ptr,
                                                         const int32_t *__restrict__ cols,
@@ -90,35 +127,7 @@ __global__ void __launch_bounds__(kThreads) spmm_rows_d(int64_t N, const int64_t
     for (int c = 0; c < D; ++c) sums[c] = 0;
     if (i < N) {
         float acc[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] = 0.f;
-        const int64_t p0 = row_ptr[i], p1 = row_ptr[i + 1];
-        for (int64_t p = p0; p < p1; p += 8) {
-            int32_t cc[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cc[k] = (p + k < p1) ? __ldg(cols + p + k) : -1;
-            float yv[8][D];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                if (cc[k] >= 0) {
-                    if constexpr (D == 2) {
-                        const float2 t = __ldg(reinterpret_cast<const float2 *>(Yold) + cc[k]);
-                        yv[k][0] = t.x;
-                        yv[k][1] = t.y;
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < D; ++c) yv[k][c] = __ldg(Yold + (int64_t)cc[k] * D + c);
-                    }
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (cc[k] >= 0) {
-#pragma unroll
-                    for (int c = 0; c < D; ++c)
-                        acc[c] = __fadd_rn(acc[c], __fmul_rn(alpha, yv[k][c]));
-                }
-        }
+        row_average<D>(row_ptr, cols, alpha, Yold, i, acc);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
             Ynew[i * D + c] = acc[c];
@@ -220,6 +229,29 @@ __global__ void __launch_bounds__(kThreads) spmm_rows_batched(
     block_partial(sums, d, part);
 }
 
+template <int D>
+__global__ void __launch_bounds__(kThreads) spmm_rows_batched_d(
+    const int64_t *__restrict__ tp, const int64_t *__restrict__ off, int B,
+    const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ cols, float alpha,
+    const float *__restrict__ Yold, float *__restrict__ Ynew, double *__restrict__ part) {
+    int p;
+    int64_t row_end;
+    const int64_t i = tile_rows(tp, off, B, p, row_end);
+    double sums[kMaxDim];
+#pragma unroll
+    for (int c = 0; c < D; ++c) sums[c] = 0;
+    if (i < row_end) {
+        float acc[D];
+        row_average<D>(row_ptr, cols, alpha, Yold, i, acc);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            Ynew[i * D + c] = acc[c];
+            sums[c] = acc[c];
+        }
+    }
+    block_partial(sums, D, part);
+}
+
 __global__ void __launch_bounds__(kThreads) centred_squares_batched(
     const int64_t *__restrict__ tp, const int64_t *__restrict__ off, int B, int d,
     const float *__restrict__ Y, const float *__restrict__ mean, double *__restrict__ part) {
@@ -302,8 +334,27 @@ void run_init_embedding_batched(int64_t total_rows, int d, const int64_t *off, c
     for (int ep = 0; ep < n_init_epochs; ++ep) {
         const float *y_old = bufs[ep % 2];
         float *y_new = bufs[(ep + 1) % 2];
-        NCVIS_LAUNCH(spmm_rows_batched, (unsigned)n_tiles, kThreads, 0, s, tp, off, B, d, row_ptr,
-                     cols, alpha, y_old, y_new, part);
+        switch (d) {
+            case 1:
+                NCVIS_LAUNCH(spmm_rows_batched_d<1>, (unsigned)n_tiles, kThreads, 0, s, tp, off, B,
+                             row_ptr, cols, alpha, y_old, y_new, part);
+                break;
+            case 2:
+                NCVIS_LAUNCH(spmm_rows_batched_d<2>, (unsigned)n_tiles, kThreads, 0, s, tp, off, B,
+                             row_ptr, cols, alpha, y_old, y_new, part);
+                break;
+            case 3:
+                NCVIS_LAUNCH(spmm_rows_batched_d<3>, (unsigned)n_tiles, kThreads, 0, s, tp, off, B,
+                             row_ptr, cols, alpha, y_old, y_new, part);
+                break;
+            case 4:
+                NCVIS_LAUNCH(spmm_rows_batched_d<4>, (unsigned)n_tiles, kThreads, 0, s, tp, off, B,
+                             row_ptr, cols, alpha, y_old, y_new, part);
+                break;
+            default:
+                NCVIS_LAUNCH(spmm_rows_batched, (unsigned)n_tiles, kThreads, 0, s, tp, off, B, d,
+                             row_ptr, cols, alpha, y_old, y_new, part);
+        }
         NCVIS_LAUNCH(finish_stat_batched, B, 256, 0, s, part, tp, off, d, 0, mean);
         NCVIS_LAUNCH(centred_squares_batched, (unsigned)n_tiles, kThreads, 0, s, tp, off, B, d,
                      y_new, mean, part);
