@@ -42,6 +42,21 @@ struct Layout {
     }
 };
 
+// A stream-ordered device allocation freed when it goes out of scope, on
+// every exit path (errors included).
+struct StreamBuffer {
+    void *p = nullptr;
+    cudaStream_t s;
+    StreamBuffer(size_t bytes, cudaStream_t st) : s(st) {
+        NCVIS_CUDA(cudaMallocAsync(&p, std::max<size_t>(bytes, 1), s));
+    }
+    StreamBuffer(const StreamBuffer &) = delete;
+    StreamBuffer &operator=(const StreamBuffer &) = delete;
+    ~StreamBuffer() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 struct Events {
     cudaEvent_t ev[10];
     Events() {
@@ -871,8 +886,8 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         const size_t o_cd = L.take(sizeof(float) * N * C);
         const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
         const size_t o_Xc = fold ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
-        char *base = nullptr;
-        NCVIS_CUDA(cudaMallocAsync((void **)&base, L.total, s));
+        StreamBuffer buf(L.total, s);
+        char *base = (char *)buf.p;
         NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int) * 2, s));
         __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
         __nv_bfloat16 *Xc = fold ? (__nv_bfloat16 *)(base + o_Xc) : nullptr;
@@ -882,20 +897,12 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         int bad = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&bad, base + o_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
-        if (bad) {
-            cudaFreeAsync(base, s);
-            throw Error(kInvalidArgument, "knn: input contains non-finite values");
-        }
+        require(!bad, "knn: input contains non-finite values");
         NCVIS_CUDA(cudaMemsetAsync(d_inds, 0xff, sizeof(int32_t) * N * k, s));
         if (ivf) {
-            try {
-                run_knn_ivf((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
-                            plan_ivf((int64_t)N, lists, probe), 42, (int32_t *)(base + o_ci),
-                            (int *)(base + o_flag) + 1, s);
-            } catch (...) {
-                cudaFreeAsync(base, s);
-                throw;
-            }
+            run_knn_ivf((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
+                        plan_ivf((int64_t)N, lists, probe), 42, (int32_t *)(base + o_ci),
+                        (int *)(base + o_flag) + 1, s);
         } else if (bf16) {
             launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
                                  (int32_t *)(base + o_ci), (float *)(base + o_cd),
@@ -904,10 +911,8 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
             NCVIS_CUDA(cudaMemcpyAsync(&timeout, (int *)(base + o_flag) + 1, sizeof(int),
                                        cudaMemcpyDeviceToHost, s));
             NCVIS_CUDA(cudaStreamSynchronize(s));
-            if (timeout) {
-                cudaFreeAsync(base, s);
-                throw Error(kDeviceTimeout, "knn: the tensor-core kernel timed out waiting on a barrier");
-            }
+            require(!timeout, "knn: the tensor-core kernel timed out waiting on a barrier",
+                    kDeviceTimeout);
         } else {
             launch_knn_select_f32((float *)(base + o_Xp), (float *)(base + o_sqn), (int64_t)N,
                                   (int)D, distance, kp, (int32_t *)(base + o_ci),
@@ -915,7 +920,6 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         }
         launch_rerank((float *)(base + o_Xp), (int64_t)N, (int)D, distance,
                       (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s);
-        NCVIS_CUDA(cudaFreeAsync(base, s));
     }
 }
 
@@ -946,17 +950,9 @@ int ncvis_symmetrize_device(size_t N, size_t k, const int32_t *d_inds, const flo
                 "symmetrize: null pointer");
         require(N >= 1 && k >= 1, "symmetrize: empty table");
         cudaStream_t s = (cudaStream_t)stream;
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, symmetrize_workspace_bytes((int64_t)N, (int)k), s));
-        int64_t E = 0;
-        try {
-            E = run_symmetrize((int64_t)N, (int)k, d_inds, d_dists, ws, d_row_ptr, d_cols, d_vals,
-                               d_src, s);
-        } catch (...) {
-            cudaFreeAsync(ws, s);
-            throw;
-        }
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+        StreamBuffer ws(symmetrize_workspace_bytes((int64_t)N, (int)k), s);
+        const int64_t E = run_symmetrize((int64_t)N, (int)k, d_inds, d_dists, ws.p, d_row_ptr,
+                                         d_cols, d_vals, d_src, s);
         *n_edges = (size_t)E;
     });
 }
@@ -981,11 +977,9 @@ int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
         require(rp[N] < (int64_t(1) << 31), "init_embedding: too many edges");
         require(indices_in_range(d_cols, rp[N], (int64_t)N, s),
                 "init_embedding: a column index is outside [0, N)");
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, init_workspace_bytes((int64_t)N, (int)d), s));
+        StreamBuffer ws(init_workspace_bytes((int64_t)N, (int)d), s);
         run_init_embedding((int64_t)N, (int)d, d_row_ptr, d_cols, seed, n_init_epochs, alpha, dY,
-                           ws, s);
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+                           ws.p, s);
     });
 }
 
@@ -1007,12 +1001,10 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "optimize: an edge endpoint is outside [0, N)");
         if (chains <= 0) chains = sgd_default_chains((int64_t)E, (int64_t)N, (int)d);
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
+        StreamBuffer ws(sgd_workspace_bytes(chains), s);
         SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,
                   a, b, alpha, alpha_Q};
-        run_sgd_hogwild(g, epoch_begin, epoch_end, n_noise, chains, ws, s);
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+        run_sgd_hogwild(g, epoch_begin, epoch_end, n_noise, chains, ws.p, s);
     });
 }
 
@@ -1039,12 +1031,10 @@ int ncvis_optimize_staged_device(size_t N, size_t d, size_t E, const int32_t *d_
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "optimize_staged: an edge endpoint is outside [0, N)");
         if (chains <= 0) chains = sgd_window_default_chains((int64_t)E, (int64_t)N, (int)d);
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, sgd_workspace_bytes(chains), s));
+        StreamBuffer ws(sgd_workspace_bytes(chains), s);
         SgdArgs g{(int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, seed, n_epochs,
                   a, b, alpha, alpha_Q};
-        run_sgd_window(g, epoch_begin, epoch_end, n_noise, chains, round_edges, ws, s);
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+        run_sgd_window(g, epoch_begin, epoch_end, n_noise, chains, round_edges, ws.p, s);
     });
 }
 
@@ -1060,15 +1050,14 @@ int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const
         require(edge_begin <= edge_end && epoch >= 0 && epoch < n_epochs,
                 "optimize_replay: bad edge or epoch range");
         cudaStream_t s = (cudaStream_t)stream;
-        int *err = nullptr;
-        NCVIS_CUDA(cudaMallocAsync((void **)&err, sizeof(int), s));
+        StreamBuffer err_buf(sizeof(int), s);
+        int *err = (int *)err_buf.p;
         NCVIS_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
         SgdArgs g{(int64_t)N, (int)d, 0, d_src, d_dst, dY, dQ, 0, n_epochs, a, b, alpha, alpha_Q};
         launch_sgd_replay(g, epoch, n_noise_epoch, (int64_t)edge_begin, (int64_t)edge_end,
                           d_stream, (int64_t)stream_offset, err, s);
         int herr = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-        NCVIS_CUDA(cudaFreeAsync(err, s));
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(herr == 0, "optimize_replay: an index outside [0, N) was met; replay stopped");
     });
@@ -1086,11 +1075,9 @@ int ncvis_nce_loss_device(size_t N, size_t d, size_t E, const int32_t *d_src, co
         cudaStream_t s = (cudaStream_t)stream;
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "nce_loss: an edge endpoint is outside [0, N)");
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));
+        StreamBuffer ws(nce_workspace_bytes((int64_t)E), s);
         run_nce(0, (int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, (int)n_noise, a, b, seed,
-                tag, edge_offset, nullptr, nullptr, d_loss, ws, s);
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+                tag, edge_offset, nullptr, nullptr, d_loss, ws.p, s);
     });
 }
 
@@ -1107,11 +1094,9 @@ int ncvis_nce_grad_device(size_t N, size_t d, size_t E, const int32_t *d_src, co
         cudaStream_t s = (cudaStream_t)stream;
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
                 "nce_grad: an edge endpoint is outside [0, N)");
-        void *ws = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&ws, nce_workspace_bytes((int64_t)E), s));
+        StreamBuffer ws(nce_workspace_bytes((int64_t)E), s);
         run_nce(1, (int64_t)N, (int)d, (int64_t)E, d_src, d_dst, dY, dQ, (int)n_noise, a, b, seed,
-                tag, edge_offset, d_scale, d_gradY, d_gradQ, ws, s);
-        NCVIS_CUDA(cudaFreeAsync(ws, s));
+                tag, edge_offset, d_scale, d_gradY, d_gradQ, ws.p, s);
     });
 }
 

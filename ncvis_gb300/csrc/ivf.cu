@@ -172,28 +172,36 @@ HostWork all_pairs_work(int64_t nq, int64_t nc) {
     return w;
 }
 
-// Device copies of a work list (stream-ordered allocations, freed by the caller).
-struct DeviceWork {
-    int64_t *begin = nullptr;
-    TcItem *items = nullptr;
+// Stream-ordered device allocations freed when the owner goes out of scope
+// (on every exit path, errors included).
+struct DeviceArena {
+    cudaStream_t s;
+    std::vector<void *> ptrs;
+    explicit DeviceArena(cudaStream_t st) : s(st) {}
+    DeviceArena(const DeviceArena &) = delete;
+    DeviceArena &operator=(const DeviceArena &) = delete;
+    ~DeviceArena() {
+        for (void *p : ptrs) cudaFreeAsync(p, s);
+    }
+    template <typename T>
+    T *alloc(size_t count) {
+        void *p = nullptr;
+        NCVIS_CUDA(cudaMallocAsync(&p, sizeof(T) * std::max<size_t>(count, 1), s));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
 };
 
-DeviceWork upload(const HostWork &w, cudaStream_t s) {
-    DeviceWork d;
-    NCVIS_CUDA(cudaMallocAsync((void **)&d.begin, sizeof(int64_t) * w.begin.size(), s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&d.items, sizeof(TcItem) * std::max<size_t>(w.items.size(), 1), s));
-    NCVIS_CUDA(cudaMemcpyAsync(d.begin, w.begin.data(), sizeof(int64_t) * w.begin.size(),
-                               cudaMemcpyHostToDevice, s));
+// Device copy of a work list, owned by `arena`.
+TcWork upload(const HostWork &w, const int32_t *map, DeviceArena &arena) {
+    int64_t *begin = arena.alloc<int64_t>(w.begin.size());
+    TcItem *items = arena.alloc<TcItem>(w.items.size());
+    NCVIS_CUDA(cudaMemcpyAsync(begin, w.begin.data(), sizeof(int64_t) * w.begin.size(),
+                               cudaMemcpyHostToDevice, arena.s));
     if (!w.items.empty())
-        NCVIS_CUDA(cudaMemcpyAsync(d.items, w.items.data(), sizeof(TcItem) * w.items.size(),
-                                   cudaMemcpyHostToDevice, s));
-    return d;
-}
-
-void release(DeviceWork &d, cudaStream_t s) {
-    if (d.begin) cudaFreeAsync(d.begin, s);
-    if (d.items) cudaFreeAsync(d.items, s);
-    d = DeviceWork{};
+        NCVIS_CUDA(cudaMemcpyAsync(items, w.items.data(), sizeof(TcItem) * w.items.size(),
+                                   cudaMemcpyHostToDevice, arena.s));
+    return TcWork{w.ctas, begin, items, map};
 }
 
 void check_timeout(int *flag, cudaStream_t s) {
@@ -225,22 +233,18 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
     const bool fold = tp.fold;
     const int C = ip.C, ldb = tp.ldb;
     const int Rp = ip.probe > 32 ? 64 : 32;  // nearest cells listed per cell
-    float *cent = nullptr, *sums = nullptr;
-    int *counts = nullptr, *cursor = nullptr;
-    __nv_bfloat16 *Cq = nullptr, *Cc = nullptr, *Xs = nullptr, *Xcs = nullptr;
-    int32_t *pcand = nullptr, *perm = nullptr;
-    int64_t *d_starts = nullptr;
-    NCVIS_CUDA(cudaMallocAsync((void **)&cent, sizeof(float) * C * D, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&sums, sizeof(float) * C * D, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&counts, sizeof(int) * C, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&cursor, sizeof(int) * C, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&Cq, sizeof(__nv_bfloat16) * C * ldb, s));
-    if (fold) NCVIS_CUDA(cudaMallocAsync((void **)&Cc, sizeof(__nv_bfloat16) * C * ldb, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&pcand, sizeof(int32_t) * C * Rp, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&perm, sizeof(int32_t) * N, s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&d_starts, sizeof(int64_t) * (C + 1), s));
-    NCVIS_CUDA(cudaMallocAsync((void **)&Xs, sizeof(__nv_bfloat16) * N * ldb, s));
-    if (fold) NCVIS_CUDA(cudaMallocAsync((void **)&Xcs, sizeof(__nv_bfloat16) * N * ldb, s));
+    DeviceArena arena(s);
+    float *cent = arena.alloc<float>((size_t)C * D);
+    float *sums = arena.alloc<float>((size_t)C * D);
+    int *counts = arena.alloc<int>(C);
+    int *cursor = arena.alloc<int>(C);
+    __nv_bfloat16 *Cq = arena.alloc<__nv_bfloat16>((size_t)C * ldb);
+    __nv_bfloat16 *Cc = fold ? arena.alloc<__nv_bfloat16>((size_t)C * ldb) : nullptr;
+    int32_t *pcand = arena.alloc<int32_t>((size_t)C * Rp);
+    int32_t *perm = arena.alloc<int32_t>((size_t)N);
+    int64_t *d_starts = arena.alloc<int64_t>((size_t)C + 1);
+    __nv_bfloat16 *Xs = arena.alloc<__nv_bfloat16>((size_t)N * ldb);
+    __nv_bfloat16 *Xcs = fold ? arena.alloc<__nv_bfloat16>((size_t)N * ldb) : nullptr;
     const __nv_bfloat16 *Ccand = fold ? Cc : Cq;
 
     // 1. k-means: ip.iters moves of the centroids, each after an assignment.
@@ -252,9 +256,7 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
     NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
     KnnTcPlan ap = tp;
     ap.R = 32;
-    const HostWork aw = all_pairs_work(N, C);
-    DeviceWork adw = upload(aw, s);
-    const TcWork awork{aw.ctas, adw.begin, adw.items, nullptr};
+    const TcWork awork = upload(all_pairs_work(N, C), nullptr, arena);
     const int normalise = (dist == kCosine || dist == kCorrelation) ? 1 : 0;
     for (int pass = 0;; ++pass) {
         NCVIS_LAUNCH(ivf_centroid_rows, warps_c, 256, 0, s, cent, C, D, ldb, fold ? 1 : 0, Cq,
@@ -266,18 +268,14 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
                      32, C, sums, counts);
         NCVIS_LAUNCH(ivf_update, warps_c, 256, 0, s, cent, sums, counts, C, D, normalise);
     }
-    release(adw, s);
     check_timeout(timeout_flag, s);
 
     // Nearest cells of each cell (its own first for the spaces where a
     // centroid is its own best match; the work list adds it where not).
-    const HostWork pw = all_pairs_work(C, C);
-    DeviceWork pdw = upload(pw, s);
     KnnTcPlan pp = tp;
     pp.R = Rp;
     launch_knn_select_tc_pair(Cq, C, Ccand, C, nullptr, pp, true, pcand, timeout_flag, s,
-                              TcWork{pw.ctas, pdw.begin, pdw.items, nullptr});
-    release(pdw, s);
+                              upload(all_pairs_work(C, C), nullptr, arena));
 
     // 2. Counting sort by cell.
     NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
@@ -360,15 +358,9 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
     }
 
     // 4. The search over the sorted rows, written in original numbering.
-    DeviceWork sdw = upload(sw, s);
     launch_knn_select_tc_pair(Xs, N, fold ? Xcs : Xs, N, nullptr, tp, true, cand_i, timeout_flag,
-                              s, TcWork{sw.ctas, sdw.begin, sdw.items, perm});
-    release(sdw, s);
+                              s, upload(sw, perm, arena));
     check_timeout(timeout_flag, s);
-    for (void *ptr : {(void *)cent, (void *)sums, (void *)counts, (void *)cursor, (void *)Cq,
-                      (void *)Cc, (void *)pcand, (void *)perm, (void *)d_starts, (void *)Xs,
-                      (void *)Xcs})
-        if (ptr) cudaFreeAsync(ptr, s);
 }
 
 }  // namespace ncvis_gpu
