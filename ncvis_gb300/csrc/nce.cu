@@ -167,9 +167,10 @@ __device__ __forceinline__ void add_row(float *dY, int64_t i, const Row<D> &g) {
 
 // nce_edges for d = D with rows of 4 D bytes aligned to their vector width:
 // y_i read once per edge and its gradient summed in registers, noise drawn
-// two samples per Philox block (the same indices as noise_index), the y_o
-// gradients applied as L2 reductions, per-thread sums in FP32 (1 + nu terms)
-// and the block sums in FP64.
+// two samples per Philox block (the same indices as noise_index) and the rows
+// of several samples loaded per round trip, the y_o gradients applied as L2
+// reductions, per-thread sums in FP32 (1 + nu terms, in sample order) and the
+// block sums in FP64.
 template <int D>
 __global__ void __launch_bounds__(kThreads) nce_edges_t(int mode, int64_t E, uint32_t N,
                                                         const int32_t *__restrict__ src,
@@ -190,30 +191,37 @@ __global__ void __launch_bounds__(kThreads) nce_edges_t(int mode, int64_t E, uin
         Row<D> gi;
 #pragma unroll
         for (int q = 0; q < D; ++q) gi.v[q] = 0.f;
-        uint32_t second = 0;
-        for (int s = 0; s <= c.nu; ++s) {
-            uint32_t o;
-            if (s == 0) {
-                o = (uint32_t)dst[e];
-            } else if (((s - 1) & 1) == 0) {
-                noise_pair(c.k0, c.k1, edge_offset + (uint64_t)e, c.tag, (uint32_t)(s - 1) >> 1,
-                           (uint32_t)i, N, o, second);
-            } else {
-                o = second;
-            }
-            const Row<D> yo = load_row<D>(Y, o);
+        // Rows loaded a group at a time (Y does not change during the loss):
+        // the positive row together with the first group of noise rows, then
+        // kG noise rows per round trip, noise samples 2p, 2p+1 from Philox
+        // block p (noise_pair, the indices noise_index gives).
+        constexpr int kG = D <= 4 ? 8 : (D <= 8 ? 4 : 2);
+        const uint64_t eg = edge_offset + (uint64_t)e;
+        uint32_t o[kG];
+        Row<D> yo[kG];
+        auto fetch = [&](int n0) {
+#pragma unroll
+            for (int t = 0; t < kG; t += 2)
+                if (n0 + t < c.nu)
+                    noise_pair(c.k0, c.k1, eg, c.tag, (uint32_t)(n0 + t) >> 1, (uint32_t)i, N, o[t],
+                               o[t + 1]);
+#pragma unroll
+            for (int t = 0; t < kG; ++t)
+                if (n0 + t < c.nu) yo[t] = load_row<D>(Y, o[t]);
+        };
+        auto sample = [&](uint32_t ot, const Row<D> &yr, bool positive) {
             Row<D> diff;
             float d2 = 0.f;
 #pragma unroll
             for (int q = 0; q < D; ++q) {
-                diff.v[q] = yi.v[q] - yo.v[q];
+                diff.v[q] = yi.v[q] - yr.v[q];
                 d2 = fmaf(diff.v[q], diff.v[q], d2);
             }
             float loss, w, g;
-            sample_terms(d2, s == 0, c, loss, w, g);
+            sample_terms(d2, positive, c, loss, w, g);
             acc_loss += loss;
             acc_dq += w;
-            if (mode == 1 && (int64_t)o != i) {
+            if (mode == 1 && (int64_t)ot != i) {
                 const float gs = g * sc;
                 Row<D> go;
 #pragma unroll
@@ -221,8 +229,20 @@ __global__ void __launch_bounds__(kThreads) nce_edges_t(int mode, int64_t E, uin
                     gi.v[q] = fmaf(gs, diff.v[q], gi.v[q]);
                     go.v[q] = -gs * diff.v[q];
                 }
-                add_row<D>(dY, o, go);
+                add_row<D>(dY, ot, go);
             }
+        };
+        const uint32_t oj = (uint32_t)dst[e];
+        const Row<D> yj = load_row<D>(Y, oj);
+        if (c.nu > 0) fetch(0);
+        sample(oj, yj, true);
+        for (int n0 = 0; n0 < c.nu; n0 += kG) {
+#pragma unroll
+            for (int t = 0; t < kG; ++t) {
+                if (n0 + t >= c.nu) break;
+                sample(o[t], yo[t], false);
+            }
+            if (n0 + kG < c.nu) fetch(n0 + kG);
         }
         if (mode == 1) add_row<D>(dY, i, gi);
     }
