@@ -329,8 +329,7 @@ def run_ours(args):
 
     L = _lib.lib()
     stage_list = []
-    clocks_path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv") \
-        if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/ncvis_clocks_{os.getpid()}.csv"
+    clocks_path = os.environ.get("NCVIS_CLOCKS_CSV", f"/tmp/ncvis_clocks_rank{rank}_{os.getpid()}.csv")
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(dev)
     torch.cuda.synchronize()
