@@ -19,8 +19,12 @@
 //     qualifying candidates go to a per-row queue in shared memory, which the
 //     warp inserts into the rows' register-resident sorted lists in lockstep
 //     rounds (R compare-exchanges each) when a queue passes half full;
-//   * a CTA takes query tiles round-robin over one problem, or, for many
-//     problems in one launch, from a work list giving each tile its rows;
+//   * a CTA takes query tiles round-robin over one problem, or items from its
+//     own work list: an item is a query tile's rows and one candidate range
+//     (masked at both ends), and may continue the previous item's tile, so
+//     one tile's lists are built over several ranges (batched problems: the
+//     tile's own problem; the inverted file: the tile's probed cells), with
+//     an optional map from sorted rows back to the caller's numbering;
 //   * squared L2 with D <= 126 folds the candidate norms into the product:
 //     candidates come from a second BF16 copy whose columns D, D + 1 hold
 //     -|c|^2 / 2 as a BF16 high and low part, the queries' copy 1, 1 there, so
