@@ -63,7 +63,8 @@ typedef enum ncvis_distance {
 /* Constructor arguments of ncvis::NCVis (src/ncvis.hpp:54), same meaning.
  * M and ef_construction configure HNSW in the reference and are accepted and
  * ignored here (the kNN is exact).  n_threads bounds host-side work only.
- * n_noise: n_epochs entries (copied at create), or NULL for 3 per epoch. */
+ * n_noise: n_epochs entries (copied at create), or NULL for 3 per epoch;
+ * each at most 2^24 (16,777,216), larger values are refused. */
 typedef struct ncvis_params {
     size_t d;
     size_t n_threads;
@@ -187,7 +188,7 @@ int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
 
 /* Parallel (Hogwild) NCE SGD over epochs [epoch_begin, epoch_end) of an
  * n_epochs schedule; Y and *dQ (device float) updated in place.  n_noise:
- * host array of n_epochs entries.  chains: 0 = automatic. */
+ * host array of n_epochs entries, each at most 2^24.  chains: 0 = automatic. */
 int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
                           const int32_t *d_dst, float *dY, float *dQ, uint64_t seed,
                           int epoch_begin, int epoch_end, int n_epochs, const size_t *n_noise,
@@ -196,7 +197,7 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
 /* The same optimizer with its noise samples staged in shared memory
  * (NCVis::optimize, src/ncvis.cpp:275-352, with the noise draw of :300
  * restated): the chains run their edges in rounds of round_edges edges
- * (0 = 8); per round each block of chains copies a window of Y (4096 rows
+ * (0 = 16; rounded up to a multiple of 4); per round each block of chains copies a window of Y (4096 rows
  * for d <= 2, 2048 for d = 3 and 4, in segments of 256 consecutive rows,
  * each starting at a uniform row and wrapping at N) into shared memory and draws every noise sample of the round uniformly
  * from the window, so each noise row stays uniform over the other N - 1

@@ -48,14 +48,21 @@ def find_ab_params(spread: float = 1.0, min_dist: float = 0.1):
 
 def default_noise_plan(n_epochs: int, n_negative: int = 5) -> np.ndarray:
     """Noise samples per epoch rising as the cube of training progress and
-    summing to about n_epochs * n_negative, at least 1 (wrapper/ncvis.pyx:103-112)."""
+    summing to about n_epochs * n_negative, at least 1 (wrapper/ncvis.pyx:103-112).
+    With one epoch the reference's plan is 0 / 0, and its cast of NaN to uintp
+    depends on the machine (2^63 on x86-64, 0 and so 1 on Arm); here it is 1."""
     plan = np.linspace(0, 1, n_epochs)
     plan = plan ** 3
-    plan /= plan.sum()
-    plan *= n_epochs * n_negative
+    total = plan.sum()
+    if total > 0:
+        plan /= total
+        plan *= n_epochs * n_negative
     plan = plan.round().astype(np.uintp)
     plan[plan < 1] = 1
     return plan
+
+
+MAX_NOISE = 1 << 24  # noise samples per edge and epoch the engine accepts
 
 
 DISTANCES = {
@@ -88,11 +95,17 @@ class NCVis:
                 raise ValueError(
                     "n_noise should have exactly one dimension, but shape {} was passed".format(
                         n_noise.shape))
+            if n_noise.size and (n_noise.min() < 0 or n_noise.max() > MAX_NOISE):
+                raise ValueError("n_noise entries should be in [0, {}], but [{}, {}] was passed"
+                                 .format(MAX_NOISE, n_noise.min(), n_noise.max()))
             negative_plan = n_noise.astype(np.uintp)
             n_epochs = negative_plan.size
         elif type(n_noise) is int:
             if n_noise < 1:
                 raise ValueError("n_noise should be at least 1, but {} was passed".format(n_noise))
+            if n_noise > MAX_NOISE:
+                raise ValueError("n_noise should be at most {}, but {} was passed".format(
+                    MAX_NOISE, n_noise))
             negative_plan = np.full(n_epochs, n_noise).astype(np.uintp)
         else:
             raise ValueError("n_noise has unsupported type")

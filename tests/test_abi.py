@@ -57,3 +57,24 @@ def test_cpp_header_compiles():
     os.remove(out)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ok" in r.stdout
+
+
+def test_create_refuses_noise_above_bound():
+    """ncvis_create checks the noise plan on the host (no GPU call): an entry
+    above 2^24 returns NULL with a message; 2^24 itself is accepted."""
+    import ctypes as C
+    from ncvis_gb300 import _lib
+    L = _lib.lib()
+    for top, ok in (((1 << 24) + 1, False), (1 << 24, True), ((1 << 63), False)):
+        plan = (C.c_size_t * 3)(1, top, 2)
+        p = _lib.NcvisParams(d=2, n_threads=1, n_neighbors=15, M=16, ef_construction=200,
+                             random_seed=42, n_epochs=3, n_init_epochs=20, a=1.0, b=1.0,
+                             alpha=1.0, alpha_Q=1.0, n_noise=C.cast(plan, C.POINTER(C.c_size_t)),
+                             distance=0)
+        h = L.ncvis_create(C.byref(p), None)
+        if ok:
+            assert h
+            L.ncvis_destroy(h)
+        else:
+            assert not h
+            assert b"n_noise entries must be at most 16777216" in L.ncvis_get_last_error()

@@ -30,7 +30,12 @@ def test_noise_plan_50():
 
 
 def test_noise_plan_small():
-    assert default_noise_plan(1).tolist() == [1] or default_noise_plan(1).min() >= 1
+    # One epoch: the reference's 0 / 0 would cast NaN (2^63 on x86-64).
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        assert default_noise_plan(1).tolist() == [1]
+        assert default_noise_plan(0).tolist() == []
     assert default_noise_plan(3).min() >= 1
 
 
@@ -41,6 +46,14 @@ def test_n_noise_errors():
         ncvis.NCVis(n_noise=0)
     with pytest.raises(ValueError, match="unsupported type"):
         ncvis.NCVis(n_noise=1.5)
+    # A negative entry would wrap to 2^64 - 1 in the uintp plan.
+    with pytest.raises(ValueError, match="should be in"):
+        ncvis.NCVis(n_noise=np.array([3, -1, 3]))
+    with pytest.raises(ValueError, match="should be in"):
+        ncvis.NCVis(n_noise=np.array([3, (1 << 24) + 1]))
+    with pytest.raises(ValueError, match="at most"):
+        ncvis.NCVis(n_noise=(1 << 24) + 1)
+    assert ncvis.NCVis(n_noise=np.array([0, 1 << 24])).noise_plan.tolist() == [0, 1 << 24]
 
 
 def test_distance_error():
