@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 
 N_FULL, D_FULL, K_NN, D_EMB, EPOCHS, INIT_EPOCHS = 1_024_000, 100, 15, 2, 50, 20
 SAMPLE_N = 65_536  # CPU-baseline sample of the same generator
+SAMPLE_N_ONE_THREAD = 16_384  # its one-thread sample
 RECALL_QUERIES = 10_000  # recall@15 sample against FP64 exact search
 # DRAM bytes (read + write) of one full-size BF16 kNN-selection launch, from the
 # ncu capture in profiles/knn_select_tc_1024000x100_dram.md.
@@ -160,26 +161,28 @@ def barrier(device=None):
 
 # ------------------------------------------------------- CPU (reference) arm
 
-def cpu_sample_pipeline(threads, steps, warmup, log=print):
-    """The reference's algorithm (oracle port, all host threads) on a
-    SAMPLE_N-point sample of the workload: kNN once (brute force, reported,
+def cpu_sample_pipeline(threads, steps, warmup, log=print, n_sample=SAMPLE_N, knn_threads=0):
+    """The reference's algorithm (oracle port, `threads` host threads) on an
+    n_sample-point sample of the workload: kNN once (brute force, reported,
     not in the value), then per step symmetrize + build_edges + init +
-    optimize, extrapolated linearly to N_FULL (all four are O(E))."""
+    optimize, extrapolated linearly to N_FULL (all four are O(E)).  The
+    untimed kNN runs on knn_threads threads (default: `threads`)."""
     from oracle import oracle as O
     from ncvis_gb300.api import default_noise_plan, find_ab_params
-    X = workload(SAMPLE_N)
+    X = workload(n_sample)
     a, b = find_ab_params(1.0, 0.4)
     plan = default_noise_plan(EPOCHS).astype(np.uint64)
     t = time.perf_counter()
     Xp = O.preprocess(X, 2)
-    inds, dists = O.knn(Xp, 2, K_NN, use_f64=False, n_threads=threads)
+    knn_threads = knn_threads or threads
+    inds, dists = O.knn(Xp, 2, K_NN, use_f64=False, n_threads=knn_threads)
     t_knn = time.perf_counter() - t
     times = []
     for s in range(warmup + steps):
         t0 = time.perf_counter()
         rp, cols, _ = O.symmetrize(inds, dists, n_threads=threads)
         src = O.edges_from_csr(rp)
-        Y = O.init_embedding(SAMPLE_N, D_EMB, src, cols, 42, INIT_EPOCHS, np.float32(1 / K_NN),
+        Y = O.init_embedding(n_sample, D_EMB, src, cols, 42, INIT_EPOCHS, np.float32(1 / K_NN),
                              threads)
         O.optimize(Y, 0.0, src, cols, 42, plan, a, b, n_threads=threads)
         dt = time.perf_counter() - t0
@@ -187,17 +190,18 @@ def cpu_sample_pipeline(threads, steps, warmup, log=print):
             times.append(dt)
         log(f"cpu step {s}: {dt:.2f}s (E={src.size})")
     per_step = statistics.median(times)
-    scale = N_FULL / SAMPLE_N
+    scale = N_FULL / n_sample
     return {
         "value": per_step * scale,
         "unit": "s",
         "cores": threads,
         "kind": "port",
-        "sample": (f"{SAMPLE_N} points of the same vMF generator; symmetrize+build_edges+init+"
+        "sample": (f"{n_sample} points of the same vMF generator; symmetrize+build_edges+init+"
                    f"optimize timed ({per_step:.2f}s median of {len(times)}) and scaled by "
                    f"N_full/N_sample={scale:.2f} (O(E) stages); the reference's HNSW kNN is "
                    f"unavailable (hnswlib absent) and excluded, so this is a lower bound of its "
-                   f"fit_transform time; brute-force FP32 kNN of the sample took {t_knn:.2f}s"),
+                   f"fit_transform time; brute-force FP32 kNN of the sample took {t_knn:.2f}s "
+                   f"on {knn_threads} threads"),
         "sample_step_s": per_step,
         "knn_bruteforce_sample_s": t_knn,
         "edges_sample": int(src.size),
@@ -460,6 +464,10 @@ def run_ours(args):
     if not args.no_cpu_baseline and world == 1:
         cpu_full = cpu_sample_pipeline(os.cpu_count() or 1, 1, 0, log=lambda m: print(m, file=sys.stderr))
         cpu = {k: cpu_full[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # The same port on one thread (a smaller sample keeps it near 10 s).
+        one = cpu_sample_pipeline(1, 1, 0, log=lambda m: print(m, file=sys.stderr),
+                                  n_sample=SAMPLE_N_ONE_THREAD, knn_threads=os.cpu_count() or 1)
+        cpu["one_thread"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
         small = small_config(dev)
 
     line = {
