@@ -57,14 +57,12 @@ std::atomic<uint64_t> &launch_counter();
 // Makes `msg` the text ncvis_get_last_error() returns on this thread.
 void record_error(const char *msg);
 
+// SMs of the current device (asked each time: a process may drive several).
 inline int num_sms() {
-    static int sms = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 1;
-    }();
-    return sms;
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
 }
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }

@@ -355,12 +355,10 @@ void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int 
                            const KnnPlan &plan, int32_t *cand_i, float *cand_d, cudaStream_t s,
                            const Segments &seg) {
     const size_t smem = select_smem_bytes(plan.R);
-    static size_t configured = 0;
-    if (smem > configured) {
-        NCVIS_CUDA(cudaFuncSetAttribute(knn_select_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-        configured = smem;
-    }
+    // Set on every launch: the attribute is per device, and a cached flag
+    // would race between host threads running different engines.
+    NCVIS_CUDA(cudaFuncSetAttribute(knn_select_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
     const int64_t tiles = seg.B > 0 ? seg.n_tiles : (int64_t)ceil_div(N, BM);
     dim3 grid((unsigned)tiles, plan.splits);
     NCVIS_LAUNCH(knn_select_f32, grid, NT, smem, s, Xp, sqnorm, N, D, dist, plan.R, plan.splits,
@@ -372,22 +370,19 @@ void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *c
     require(C <= 1024, "rerank: too many candidates per point");
     const int warps = 4;
     const size_t smem = (size_t)warps * C * 8;
-    static size_t configured = 0;
-    if (smem > configured) {
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_CUDA(cudaFuncSetAttribute(rerank_rows<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
     const unsigned grid = ceil_div(N, warps);
+    // The shared-memory attribute is set on every launch (per device; no
+    // cached flag shared between host threads).
+    auto go = [&](auto kernel) {
+        NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_LAUNCH(kernel, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists);
+    };
     switch ((D + 31) / 32) {
-        case 1: NCVIS_LAUNCH(rerank_rows<1>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
-        case 2: NCVIS_LAUNCH(rerank_rows<2>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
-        case 3: NCVIS_LAUNCH(rerank_rows<3>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
-        case 4: NCVIS_LAUNCH(rerank_rows<4>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists); break;
-        default: NCVIS_LAUNCH(rerank_rows<0>, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists);
+        case 1: go(rerank_rows<1>); break;
+        case 2: go(rerank_rows<2>); break;
+        case 3: go(rerank_rows<3>); break;
+        case 4: go(rerank_rows<4>); break;
+        default: go(rerank_rows<0>);
     }
 }
 

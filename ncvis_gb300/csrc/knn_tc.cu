@@ -591,17 +591,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// The driver's tensor-map encoder, looked up once (thread-safe static
+// initialisation; a failed lookup throws and is retried on the next call).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         NCVIS_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
                                                     cudaEnableDefault, &q));
         require(q == cudaDriverEntryPointSuccess && p != nullptr,
                 "knn: cuTensorMapEncodeTiled is unavailable", kCudaError);
-        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
     return fn;
 }
 

@@ -269,12 +269,10 @@ int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists
     launch_exclusive_scan_i32_to_i64(w.indeg, w.in_off, N, w.scan, s);
     NCVIS_LAUNCH(scatter_incoming, grid, 256, 0, s, inds, nk, w.in_off, w.cursor, w.in_key);
     const size_t smem = sizeof(SortItem) * kCap * kMergeThreads;
-    static bool configured = false;
-    if (!configured) {
-        NCVIS_CUDA(cudaFuncSetAttribute(merge_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-        configured = true;
-    }
+    // Set on every launch: the attribute is per device, and a cached flag
+    // would race between host threads running different engines.
+    NCVIS_CUDA(cudaFuncSetAttribute(merge_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
     NCVIS_LAUNCH(merge_rows, ceil_div(N, kMergeThreads), kMergeThreads, smem, s, N, k, inds, dists,
                  w.in_off, w.in_key, w.items, w.out_col, w.out_val, w.kept);
     launch_exclusive_scan_i32_to_i64(w.kept, row_ptr, N, w.scan, s);
