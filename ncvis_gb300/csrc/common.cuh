@@ -38,6 +38,46 @@ inline void check_cuda(cudaError_t e, const char *what, const char *file, int li
 
 #define NCVIS_CUDA(call) ::ncvis_gpu::check_cuda((call), #call, __FILE__, __LINE__)
 
+// A stream-ordered device allocation freed when it goes out of scope, on
+// every exit path (errors included).
+struct StreamBuffer {
+    void *p = nullptr;
+    cudaStream_t s;
+    StreamBuffer(size_t bytes, cudaStream_t st) : s(st) {
+        NCVIS_CUDA(cudaMallocAsync(&p, bytes > 0 ? bytes : 1, s));
+    }
+    StreamBuffer(const StreamBuffer &) = delete;
+    StreamBuffer &operator=(const StreamBuffer &) = delete;
+    ~StreamBuffer() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
+// Two CUDA events (start, stop), destroyed when they go out of scope.
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        NCVIS_CUDA(cudaEventCreate(&a));
+        const cudaError_t e = cudaEventCreate(&b);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(a);
+            a = nullptr;
+            NCVIS_CUDA(e);
+        }
+    }
+    EventPair(const EventPair &) = delete;
+    EventPair &operator=(const EventPair &) = delete;
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    float ms() const {
+        float t = 0.f;
+        NCVIS_CUDA(cudaEventElapsedTime(&t, a, b));
+        return t;
+    }
+};
+
 inline void require(bool ok, const std::string &msg, int code = kInvalidArgument) {
     if (!ok) throw Error(code, msg);
 }

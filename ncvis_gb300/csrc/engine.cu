@@ -42,28 +42,26 @@ struct Layout {
     }
 };
 
-// A stream-ordered device allocation freed when it goes out of scope, on
-// every exit path (errors included).
-struct StreamBuffer {
-    void *p = nullptr;
-    cudaStream_t s;
-    StreamBuffer(size_t bytes, cudaStream_t st) : s(st) {
-        NCVIS_CUDA(cudaMallocAsync(&p, std::max<size_t>(bytes, 1), s));
-    }
-    StreamBuffer(const StreamBuffer &) = delete;
-    StreamBuffer &operator=(const StreamBuffer &) = delete;
-    ~StreamBuffer() {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
-
 struct Events {
-    cudaEvent_t ev[10];
+    cudaEvent_t ev[10] = {};
     Events() {
-        for (auto &e : ev) NCVIS_CUDA(cudaEventCreate(&e));
+        for (auto &e : ev) {
+            const cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) {
+                destroy();
+                NCVIS_CUDA(r);
+            }
+        }
     }
-    ~Events() {
-        for (auto &e : ev) cudaEventDestroy(e);
+    Events(const Events &) = delete;
+    Events &operator=(const Events &) = delete;
+    ~Events() { destroy(); }
+    void destroy() {
+        for (auto &e : ev)
+            if (e) {
+                cudaEventDestroy(e);
+                e = nullptr;
+            }
     }
     float ms(int a, int b) const {
         float t = 0.f;
@@ -107,22 +105,17 @@ struct Autotuner {
         if (!loaded) load();
         auto it = best.find(key);
         if (it != best.end()) return it->second;
-        cudaEvent_t a, b;
-        NCVIS_CUDA(cudaEventCreate(&a));
-        NCVIS_CUDA(cudaEventCreate(&b));
+        EventPair t;
         int choice = candidates.front();
         float best_ms = 1e30f;
         for (int c : candidates) {
-            NCVIS_CUDA(cudaEventRecord(a, s));
+            NCVIS_CUDA(cudaEventRecord(t.a, s));
             run(c);
-            NCVIS_CUDA(cudaEventRecord(b, s));
-            NCVIS_CUDA(cudaEventSynchronize(b));
-            float ms = 0.f;
-            NCVIS_CUDA(cudaEventElapsedTime(&ms, a, b));
+            NCVIS_CUDA(cudaEventRecord(t.b, s));
+            NCVIS_CUDA(cudaEventSynchronize(t.b));
+            const float ms = t.ms();
             if (ms < best_ms) best_ms = ms, choice = c;
         }
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
         best[key] = choice;
         save();
         return choice;
@@ -757,29 +750,32 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         g.Y = dY;
         g.Qs = Qs;
         g.n_epochs = p.n_epochs;
-        // The whole epoch loop as one CUDA graph, launched once.
-        cudaStream_t cs;
-        NCVIS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        NCVIS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        // The whole epoch loop as one CUDA graph, launched once; the capture
+        // stream, graph and executable graph are released on every exit path.
+        struct Captured {
+            cudaStream_t cs = nullptr;
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            ~Captured() {
+                if (exec) cudaGraphExecDestroy(exec);
+                if (graph) cudaGraphDestroy(graph);
+                if (cs) cudaStreamDestroy(cs);
+            }
+        } cap;
+        NCVIS_CUDA(cudaStreamCreateWithFlags(&cap.cs, cudaStreamNonBlocking));
+        NCVIS_CUDA(cudaStreamBeginCapture(cap.cs, cudaStreamCaptureModeThreadLocal));
         try {
-            run_epochs(g, noise.data(), cs);
+            run_epochs(g, noise.data(), cap.cs);
         } catch (...) {
-            cudaStreamEndCapture(cs, &graph);
-            if (graph) cudaGraphDestroy(graph);
-            cudaStreamDestroy(cs);
+            cudaStreamEndCapture(cap.cs, &cap.graph);
             throw;
         }
-        NCVIS_CUDA(cudaStreamEndCapture(cs, &graph));
-        NCVIS_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        NCVIS_CUDA(cudaStreamEndCapture(cap.cs, &cap.graph));
+        NCVIS_CUDA(cudaGraphInstantiate(&cap.exec, cap.graph, 0));
         NCVIS_CUDA(cudaEventRecord(ev.ev[9], s));
-        NCVIS_CUDA(cudaGraphLaunch(exec, s));
+        NCVIS_CUDA(cudaGraphLaunch(cap.exec, s));
         NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
         NCVIS_CUDA(cudaEventSynchronize(ev.ev[7]));
-        cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
-        cudaStreamDestroy(cs);
     } else {
         NCVIS_CUDA(cudaEventRecord(ev.ev[9], s));
         NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));

@@ -228,14 +228,13 @@ bool indices_in_range(const int32_t *a, int64_t n, int64_t N, cudaStream_t s) {
 // One check kernel over both arrays and one wait for its flag.
 bool edges_in_range(const int32_t *a, const int32_t *b, int64_t n, int64_t N, cudaStream_t s) {
     if (n == 0) return true;
-    int *bad = nullptr;
-    NCVIS_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), s));
+    StreamBuffer flag(sizeof(int), s);
+    int *bad = (int *)flag.p;
     NCVIS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
     const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 16 * num_sms());
     NCVIS_LAUNCH(check_pairs, grid, 256, 0, s, a, b, n, N, bad);
     int h = 0;
     NCVIS_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
-    NCVIS_CUDA(cudaFreeAsync(bad, s));
     NCVIS_CUDA(cudaStreamSynchronize(s));
     return h == 0;
 }

@@ -86,18 +86,13 @@ double time_rate(float *Y, uint32_t rows, float *sink, cudaStream_t s) {
     const int blocks = 2 * num_sms();
     const int64_t threads = (int64_t)blocks * kThreads;
     const int iters = (int)std::max<int64_t>(1, (int64_t(1) << 26) / (threads * kInFlight));
-    cudaEvent_t a, b;
-    NCVIS_CUDA(cudaEventCreate(&a));
-    NCVIS_CUDA(cudaEventCreate(&b));
+    EventPair t;
     NCVIS_LAUNCH((random_rows<D, kUpdate>), blocks, kThreads, 0, s, Y, rows, 2, sink);
-    NCVIS_CUDA(cudaEventRecord(a, s));
+    NCVIS_CUDA(cudaEventRecord(t.a, s));
     NCVIS_LAUNCH((random_rows<D, kUpdate>), blocks, kThreads, 0, s, Y, rows, iters, sink);
-    NCVIS_CUDA(cudaEventRecord(b, s));
-    NCVIS_CUDA(cudaEventSynchronize(b));
-    float ms = 0.f;
-    NCVIS_CUDA(cudaEventElapsedTime(&ms, a, b));
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    NCVIS_CUDA(cudaEventRecord(t.b, s));
+    NCVIS_CUDA(cudaEventSynchronize(t.b));
+    const float ms = t.ms();
     return (double)threads * kInFlight * iters / (ms * 1e-3);
 }
 
