@@ -87,7 +87,7 @@ typedef struct ncvis_params {
 typedef struct ncvis_options {
     int knn_precision;      /* NCVIS_KNN_FP32 | NCVIS_KNN_BF16_RERANK | NCVIS_KNN_IVF */
     int rerank_factor;      /* candidates kept per point ~ rerank_factor * k (0: 2; BF16 keeps 32 or 64) */
-    int sgd_mode;           /* NCVIS_SGD_HOGWILD | NCVIS_SGD_REPLAY */
+    int sgd_mode;           /* NCVIS_SGD_HOGWILD | NCVIS_SGD_REPLAY | NCVIS_SGD_HOGWILD_UNSTAGED */
     const int32_t *replay_stream; /* host array of noise indices in one-thread draw order (replay) */
     size_t replay_len;      /* entries in replay_stream: E * sum(n_noise) */
     void *stream;           /* cudaStream_t to run on; NULL: the engine's own stream */
@@ -136,8 +136,13 @@ int ncvis_fit_transform_device(ncvis_handle h, const float *dX, size_t N, size_t
  * NULL: every problem uses random_seed) are host arrays.  Every problem
  * follows the engine's parameters (k clamped by the smallest problem) with
  * its own kNN graph, initialisation stream, noise range and Q; the SGD epoch
- * loop of all problems runs as one captured CUDA graph.  FP32 kNN, d <= 4.
- * No reference counterpart (the reference embeds one dataset per call). */
+ * loop of all problems runs as one captured CUDA graph.  d <= 4.  The kNN
+ * follows knn_precision: exact FP32, or BF16 on the tensor cores with the
+ * exact rerank (also for NCVIS_KNN_IVF: the problems are searched exactly).
+ * The optimizer stages noise samples per problem unless sgd_mode is
+ * NCVIS_SGD_HOGWILD_UNSTAGED; NCVIS_SGD_REPLAY is refused (NCVIS_INVALID_ARGUMENT).
+ * No reference counterpart (the reference
+ * embeds one dataset per call). */
 int ncvis_fit_transform_batched_device(ncvis_handle h, const float *dX, size_t D,
                                        const int64_t *offsets, size_t n_problems,
                                        const uint64_t *seeds, float *dY);

@@ -197,7 +197,9 @@ class NCVis:
         """Embeds several independent datasets in one run (each as if it were
         embedded alone, with its own seed) and returns one Y per dataset.
         numpy inputs give numpy outputs; CUDA tensors give CUDA tensors.  The
-        neighbour count is clamped by the smallest dataset; FP32 kNN, d <= 4."""
+        neighbour count is clamped by the smallest dataset; d <= 4; the kNN
+        follows knn_precision ("ivf" searches each problem exactly); the
+        replay mode is not available here."""
         import torch
         L = _lib.lib()
         cuda_in = all(_is_cuda_tensor(x) for x in Xs)

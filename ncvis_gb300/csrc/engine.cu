@@ -508,6 +508,9 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     require(p.distance >= 0 && p.distance <= 3,
             "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
     require(p.d >= 1 && p.d <= 4, "[ncvis] batched: embedding dimension d must be in [1, 4]");
+    require(o.sgd_mode != NCVIS_SGD_REPLAY,
+            "[ncvis] batched: the replay mode (one recorded noise stream per fit) is not available "
+            "for batched problems");
     // Batched problems are small: the IVF mode runs the exact BF16 search here.
     const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK || o.knn_precision == NCVIS_KNN_IVF);
     require(((uintptr_t)dY & 7) == 0, "[ncvis] device Y must be 8-byte aligned");

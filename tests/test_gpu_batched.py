@@ -87,6 +87,10 @@ def test_batched_rejects_bad_layout(cuda):
     vis = ncvis.NCVis()
     with pytest.raises(ncvis.NcvisError, match="at least two points"):
         vis.fit_transform_batched([np.zeros((1, 3), np.float32), np.ones((5, 3), np.float32)])
+    # Replay consumes one recorded stream per fit: refused before any device work.
+    vis = ncvis.NCVis(sgd_mode="replay")
+    with pytest.raises(ncvis.NcvisError, match="replay mode"):
+        vis.fit_transform_batched(_problems([300, 400]))
 
 
 @pytest.mark.parametrize("d", [1, 2, 3, 4])
