@@ -4,7 +4,9 @@ src/knntable.cpp compiled unmodified, with a brute-force hnswlib stand-in and
 pyarrow's vendored pcg-cpp; see oracle/build_ref.sh).
 
 Run where the reference checkout exists:
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [out_dir]
+(out_dir defaults to this folder; tests/test_golden_regenerate.py writes to a
+temporary one and compares).
 Every stage runs with one OpenMP thread, the reference's deterministic form.
 The fixtures pin the oracle restatement (oracle/) and, through it, the CUDA
 engine; they are inputs and outputs only.
@@ -44,7 +46,7 @@ def ref_sym(R, inds, dists):
     return rp, cols[:E].copy(), vals[:E].copy()
 
 
-def main():
+def main(out_dir: str = HERE):
     R = O.ref()
     if R is None:
         raise SystemExit("oracle/_ref/libncvis_ref.so is missing: run oracle/build_ref.sh first")
@@ -63,7 +65,7 @@ def main():
         v = np.empty(1024, np.uint64)
         R.ref_uniform_int(seed, hi, 1024, v)
         out[f"uniform_int_{seed}_{hi}"] = v
-    np.savez_compressed(os.path.join(HERE, "rng.npz"), **out)
+    np.savez_compressed(os.path.join(out_dir, "rng.npz"), **out)
 
     # --- kNN tables and symmetrization (src/ncvis.cpp:72-153, src/knntable.cpp:24-99)
     sym = {}
@@ -102,7 +104,7 @@ def main():
         inds, dists = ref_knn(R, Xs, 0, N - 1)
         sym[f"tiny{N}_inds"], sym[f"tiny{N}_dists"] = inds, dists
         sym[f"tiny{N}_rp"], sym[f"tiny{N}_cols"], sym[f"tiny{N}_vals"] = ref_sym(R, inds, dists)
-    np.savez_compressed(os.path.join(HERE, "symmetrize.npz"), **sym)
+    np.savez_compressed(os.path.join(out_dir, "symmetrize.npz"), **sym)
 
     # --- init_embedding and optimize on the L2 graph above (src/ncvis.cpp:184-352)
     rp, cols = sym["sym_rp_0"], sym["sym_cols_0"]
@@ -122,7 +124,7 @@ def main():
         R.ref_optimize(N, d, src.shape[0], src, cols, 42, 50, plan, A_DEFAULT, B_DEFAULT, 1.0, 1.0,
                        1, Y, C.byref(q))
         emb[f"opt_d{d}_Y"], emb[f"opt_d{d}_Q"] = Y, np.float32(q.value)
-    np.savez_compressed(os.path.join(HERE, "embedding.npz"), **emb)
+    np.savez_compressed(os.path.join(out_dir, "embedding.npz"), **emb)
 
     # --- the whole pipeline (src/ncvis.cpp:354-459)
     fit = {}
@@ -133,11 +135,11 @@ def main():
         assert R.ref_fit_transform(Xf, 200, 5, 2, 1, 15, 42, 50, 20, A_DEFAULT, B_DEFAULT, 1.0,
                                    1.0, plan, dist, Y) == 0
         fit[f"Y_{dist}"] = Y
-    np.savez_compressed(os.path.join(HERE, "fit.npz"), **fit)
-    for f in sorted(os.listdir(HERE)):
+    np.savez_compressed(os.path.join(out_dir, "fit.npz"), **fit)
+    for f in sorted(os.listdir(out_dir)):
         if f.endswith(".npz"):
-            print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+            print(f, os.path.getsize(os.path.join(out_dir, f)), "bytes")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
