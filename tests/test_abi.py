@@ -78,3 +78,34 @@ def test_create_refuses_noise_above_bound():
         else:
             assert not h
             assert b"n_noise entries must be at most 16777216" in L.ncvis_get_last_error()
+
+
+def test_c_header_links_from_c99(tmp_path):
+    """include/ncvis_gb300.h is plain C (C99, strict warnings): a C program
+    includes it, links libncvis_gb300.so and runs its host-only calls."""
+    from ncvis_gb300 import _build
+    src = tmp_path / "c_check.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <string.h>\n#include "ncvis_gb300.h"\n'
+        "int main(void) {\n"
+        "    size_t plan[2] = {1, 2};\n"
+        "    ncvis_params p;\n"
+        "    ncvis_handle h;\n"
+        "    memset(&p, 0, sizeof p);\n"
+        "    p.d = 2; p.n_neighbors = 15; p.random_seed = 42; p.n_epochs = 2;\n"
+        "    p.n_init_epochs = 20; p.a = 1.f; p.b = 1.f; p.alpha = 1.f; p.alpha_Q = 1.f;\n"
+        "    p.n_noise = plan; p.distance = NCVIS_COSINE_SIMILARITY;\n"
+        "    h = ncvis_create(&p, NULL);\n"
+        "    if (!h) { printf(\"create: %s\\n\", ncvis_get_last_error()); return 1; }\n"
+        "    ncvis_destroy(h);\n"
+        "    printf(\"ok %s\\n\", ncvis_version());\n"
+        "    return 0;\n"
+        "}\n")
+    exe = str(tmp_path / "c_check")
+    lib_dir = os.path.dirname(_build.LIB)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-o", exe, "-L", lib_dir,
+                        "-lncvis_gb300", f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.startswith("ok "), r.stdout + r.stderr
