@@ -271,17 +271,17 @@ namespace {
 // loops over any value; a value above this bound is refused.
 constexpr size_t kMaxNoise = size_t(1) << 24;
 
-void check_noise(const size_t *n_noise, int begin, int end, const std::string &who) {
+void check_noise(const size_t *n_noise, int begin, int end, const std::string &prefix) {
     if (!n_noise) return;
     for (int e = begin; e < end; ++e)
         require(n_noise[e] <= kMaxNoise,
-                who + ": n_noise entries must be at most " + std::to_string(kMaxNoise) +
+                prefix + "n_noise entries must be at most " + std::to_string(kMaxNoise) +
                     " (epoch " + std::to_string(e) + ": " + std::to_string(n_noise[e]) + ")");
 }
 
 void check_params(const ncvis_params &p) {
     require(p.n_epochs >= 0, "[ncvis] n_epochs must be non-negative");
-    check_noise(p.n_noise, 0, p.n_epochs, "[ncvis]");
+    check_noise(p.n_noise, 0, p.n_epochs, "[ncvis] ");
 }
 
 template <class F>
@@ -1010,7 +1010,7 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
                 "optimize: src and dst must be 16-byte aligned");
         require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
                 "optimize: need 0 <= epoch_begin <= epoch_end <= n_epochs");
-        check_noise(n_noise, epoch_begin, epoch_end, "optimize");
+        check_noise(n_noise, epoch_begin, epoch_end, "optimize: ");
         cudaStream_t s = (cudaStream_t)stream;
         if (E == 0 || epoch_begin == epoch_end) return;
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
@@ -1041,7 +1041,7 @@ int ncvis_optimize_staged_device(size_t N, size_t d, size_t E, const int32_t *d_
                 "optimize_staged: src and dst must be 16-byte aligned");
         require(0 <= epoch_begin && epoch_begin <= epoch_end && epoch_end <= n_epochs,
                 "optimize_staged: need 0 <= epoch_begin <= epoch_end <= n_epochs");
-        check_noise(n_noise, epoch_begin, epoch_end, "optimize_staged");
+        check_noise(n_noise, epoch_begin, epoch_end, "optimize_staged: ");
         cudaStream_t s = (cudaStream_t)stream;
         if (E == 0 || epoch_begin == epoch_end) return;
         require(edges_in_range(d_src, d_dst, (int64_t)E, (int64_t)N, s),
@@ -1065,7 +1065,7 @@ int ncvis_optimize_replay_device(size_t N, size_t d, const int32_t *d_src, const
         require(N >= 2 && d >= 1 && d <= 32, "optimize_replay: need N >= 2 and 1 <= d <= 32");
         require(edge_begin <= edge_end && epoch >= 0 && epoch < n_epochs,
                 "optimize_replay: bad edge or epoch range");
-        check_noise(&n_noise_epoch, 0, 1, "optimize_replay");
+        check_noise(&n_noise_epoch, 0, 1, "optimize_replay: ");
         cudaStream_t s = (cudaStream_t)stream;
         StreamBuffer err_buf(sizeof(int), s);
         int *err = (int *)err_buf.p;
