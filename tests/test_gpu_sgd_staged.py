@@ -97,6 +97,19 @@ def test_fit_transform_uses_staged_noise_by_default(cuda):
     assert abs(T["hogwild"] - T["hogwild_unstaged"]) <= 0.01, T
 
 
+def test_rejects_noise_plan_above_bound(cuda):
+    """Both optimizer entries refuse a plan entry above 2^24 before any device
+    work (the kernels keep sample numbers in 32-bit counters)."""
+    from ncvis_gb300 import _lib, stages
+    Y = cuda.zeros((70000, 2), dtype=cuda.float32, device="cuda")
+    Q = cuda.zeros(1, dtype=cuda.float32, device="cuda")
+    src = cuda.zeros(4, dtype=cuda.int32, device="cuda")
+    for staged in (False, True):
+        with pytest.raises(_lib.NcvisError, match="n_noise entries must be at most"):
+            stages.optimize(Y, Q, src, src, 1, np.array([3, (1 << 24) + 1], np.uintp), A, B,
+                            staged=staged)
+
+
 def test_rejects_small_problems_and_wide_embeddings(cuda):
     from ncvis_gb300 import _lib, stages
     for N, d in ((1000, 2), (65536, 5)):
