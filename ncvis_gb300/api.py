@@ -129,6 +129,8 @@ class NCVis:
             raise ValueError(f"sgd_mode must be one of {sorted(_SGD_MODES)}")
         if int(ivf_lists) < 0 or int(ivf_probe) < 0:
             raise ValueError("ivf_lists and ivf_probe must be non-negative")
+        if int(rerank_factor) < 0 or int(sgd_chains) < 0:
+            raise ValueError("rerank_factor and sgd_chains must be non-negative")
 
         self.n_epochs = int(n_epochs)
         self.noise_plan = np.ascontiguousarray(negative_plan, dtype=np.uintp)

@@ -279,6 +279,24 @@ void check_noise(const size_t *n_noise, int begin, int end, const std::string &p
                     " (epoch " + std::to_string(e) + ": " + std::to_string(n_noise[e]) + ")");
 }
 
+// The options struct as a C caller may fill it: unknown modes and negative
+// counts are refused rather than falling back to a default path.
+void check_options(const ncvis_options &o) {
+    require(o.knn_precision == NCVIS_KNN_FP32 || o.knn_precision == NCVIS_KNN_BF16_RERANK ||
+                o.knn_precision == NCVIS_KNN_IVF,
+            "[ncvis] options: knn_precision must be NCVIS_KNN_FP32, NCVIS_KNN_BF16_RERANK or "
+            "NCVIS_KNN_IVF");
+    require(o.sgd_mode == NCVIS_SGD_HOGWILD || o.sgd_mode == NCVIS_SGD_REPLAY ||
+                o.sgd_mode == NCVIS_SGD_HOGWILD_UNSTAGED,
+            "[ncvis] options: sgd_mode must be NCVIS_SGD_HOGWILD, NCVIS_SGD_REPLAY or "
+            "NCVIS_SGD_HOGWILD_UNSTAGED");
+    require(o.rerank_factor >= 0 && o.sgd_chains >= 0 && o.ivf_lists >= 0 && o.ivf_probe >= 0,
+            "[ncvis] options: rerank_factor, sgd_chains, ivf_lists and ivf_probe must be "
+            "non-negative");
+    require(o.replay_len == 0 || o.replay_stream != nullptr,
+            "[ncvis] options: replay_len > 0 needs a replay_stream");
+}
+
 void check_params(const ncvis_params &p) {
     require(p.n_epochs >= 0, "[ncvis] n_epochs must be non-negative");
     check_noise(p.n_noise, 0, p.n_epochs, "[ncvis] ");
@@ -817,6 +835,7 @@ ncvis_handle ncvis_create(const ncvis_params *params, const ncvis_options *optio
             e->noise[i] = params->n_noise ? params->n_noise[i] : 3;
         e->p.n_noise = nullptr;
         if (options) {
+            check_options(*options);
             e->o = *options;
             if (options->replay_stream && options->replay_len)
                 e->replay_stream.assign(options->replay_stream, options->replay_stream + options->replay_len);
@@ -833,6 +852,7 @@ int ncvis_set_options(ncvis_handle h, const ncvis_options *options) {
     if (!h) return NCVIS_INVALID_ARGUMENT;
     return guarded(h, [&] {
         require(options != nullptr, "[ncvis] null options");
+        check_options(*options);
         h->o = *options;
         h->replay_stream.clear();
         if (options->replay_stream && options->replay_len)

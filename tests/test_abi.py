@@ -109,3 +109,31 @@ def test_c_header_links_from_c99(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.startswith("ok "), r.stdout + r.stderr
+
+
+def test_options_are_checked_on_the_host():
+    """ncvis_create and ncvis_set_options refuse unknown modes, negative counts
+    and a replay length without a stream (no GPU call is made)."""
+    import ctypes as C
+    from ncvis_gb300 import _lib
+    L = _lib.lib()
+    plan = (C.c_size_t * 2)(1, 2)
+    p = _lib.NcvisParams(d=2, n_threads=1, n_neighbors=15, M=16, ef_construction=200,
+                         random_seed=42, n_epochs=2, n_init_epochs=20, a=1.0, b=1.0, alpha=1.0,
+                         alpha_Q=1.0, n_noise=C.cast(plan, C.POINTER(C.c_size_t)), distance=0)
+    bad = [dict(knn_precision=3), dict(knn_precision=-1), dict(sgd_mode=3), dict(rerank_factor=-1),
+           dict(sgd_chains=-2), dict(ivf_lists=-1), dict(ivf_probe=-1), dict(replay_len=5)]
+    for kw in bad:
+        h = L.ncvis_create(C.byref(p), C.byref(_lib.NcvisOptions(**kw)))
+        assert not h, kw
+        assert b"[ncvis] options:" in L.ncvis_get_last_error(), kw
+    good = _lib.NcvisOptions(knn_precision=2, sgd_mode=2, rerank_factor=4, sgd_chains=8,
+                             ivf_lists=16, ivf_probe=8)
+    h = L.ncvis_create(C.byref(p), C.byref(good))
+    assert h
+    try:
+        assert L.ncvis_set_options(h, C.byref(_lib.NcvisOptions(sgd_mode=7))) == _lib.NCVIS_INVALID_ARGUMENT
+        assert b"sgd_mode" in L.ncvis_last_error(h)
+        assert L.ncvis_set_options(h, C.byref(_lib.NcvisOptions())) == 0
+    finally:
+        L.ncvis_destroy(h)

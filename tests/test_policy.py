@@ -73,6 +73,10 @@ def test_mode_errors():
         ncvis.NCVis(knn_precision="fp8")
     with pytest.raises(ValueError):
         ncvis.NCVis(sgd_mode="async")
+    with pytest.raises(ValueError, match="non-negative"):
+        ncvis.NCVis(rerank_factor=-1)
+    with pytest.raises(ValueError, match="non-negative"):
+        ncvis.NCVis(sgd_chains=-1)
 
 
 def test_distance_enum_matches_reference_order():
