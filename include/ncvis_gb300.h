@@ -205,8 +205,9 @@ int ncvis_optimize_device(size_t N, size_t d, size_t E, const int32_t *d_src,
  * (0 = 16; rounded up to a multiple of 4); per round each block of chains copies a window of Y (4096 rows
  * for d <= 2, 2048 for d = 3 and 4, in segments of 256 consecutive rows,
  * each starting at a uniform row and wrapping at N) into shared memory and draws every noise sample of the round uniformly
- * from the window, so each noise row stays uniform over the other N - 1
- * rows.  Updates of noise rows go to the window and are added to Y at the
+ * from the window, so each noise row is uniform over the N rows before the
+ * source row is excluded (a pick equal to it, probability 1/N, is redrawn
+ * within the window).  Updates of noise rows go to the window and are added to Y at the
  * end of the round.  Needs 1 <= d <= 4 and N >= 16 * window rows (65,536
  * for d <= 2, 32,768 for d = 3 and 4).  chains: 0 = automatic. */
 int ncvis_optimize_staged_device(size_t N, size_t d, size_t E, const int32_t *d_src,

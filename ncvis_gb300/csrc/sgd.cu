@@ -408,10 +408,13 @@ __global__ void reduce_q(const double *__restrict__ q_part, int blocks, int64_t 
 // the block draws W / kSegRows segment starts uniformly from [0, N), copies
 // the window rows (kSegRows consecutive rows from each start, wrapping at N) into
 // shared memory with coalesced loads, and every noise sample of the round is
-// a uniform pick among the window's rows.  A row is therefore still uniform
-// over [0, N) \ {i} for every sample (the segment start is uniform and the
-// pick within the window is uniform); what changes is only that the samples
-// of one round of one block share a window.  y_o -= dx is applied to the
+// a uniform pick among the window's rows.  Each pick is therefore uniform
+// over [0, N) (the segment start is uniform and the pick within the window
+// is uniform).  A pick equal to the edge's source i (probability 1/N) is
+// redrawn within the same window, where the reference redraws over all rows
+// (src/ncvis.cpp:299-301): rows sharing a segment with i get at most 1/N of
+// extra probability per sample.  Otherwise what changes is only that the
+// samples of one round of one block share a window.  y_o -= dx is applied to the
 // window copy; at the end of the round the window's change (current minus
 // loaded) is added to Y with coalesced L2 reductions, so updates made to the
 // same rows meanwhile by other blocks are kept.  The positive sample and y_i
