@@ -25,7 +25,7 @@ namespace ncvis_gpu {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kNceThreads;
 
 __device__ __forceinline__ float softplus(float u) {
     return fmaxf(u, 0.f) + log1pf(__expf(-fabsf(u)));

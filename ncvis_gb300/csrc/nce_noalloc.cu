@@ -8,17 +8,23 @@
 // host framework whose policy forbids allocations outside its own pool.  For
 // them, the per-block FP64 partial sums and the argument-check flag that
 // ncvis_nce_loss_device keeps in freshly allocated memory live here in one
-// file-scope device array of fixed size (kScratchDoubles doubles, 64 KiB),
+// file-scope device array of fixed size (kScratchBytes = 65,568 bytes),
 // present on every GPU that loads the library until the process exits.  A
 // call therefore accepts at most kNoAllocMaxEdges = 2^20 edges.
 //
 // Host code cannot pass the array's name to a kernel (on the host it names a
-// host-side stand-in, not device memory): the first call on each device looks
-// up the array's device address with cudaGetSymbolAddress, with that device
-// current, and caches it; make that first call before any stream capture.
-// All calls share the array and each leaves its contents behind: the check
-// flag is cleared at the start of every call (the partials are overwritten),
-// and calls whose GPU work overlaps in time race on the array.
+// host-side stand-in, not device memory).  Set-up, once per device (and again
+// if that device's context was destroyed and created anew): with the device
+// current, cudaGetSymbolAddress gives the array's device address, which is
+// kept with the context's unique id; later calls in the same context reuse
+// it.  The first call on a device does this set-up, which also loads the
+// library's device code there; make it at start-up, while memory is free,
+// and before any stream capture.  Every call waits for its stream (it reads
+// the argument-check flag back to the host).  All calls share the array and
+// each leaves its contents behind: the check flag is cleared at the start of
+// every call (the partials are overwritten), and calls whose GPU work
+// overlaps in time race on the array.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,30 +40,69 @@ namespace ncvis_gpu {
 namespace {
 
 constexpr int64_t kNoAllocMaxEdges = int64_t(1) << 20;
-constexpr int kLossThreads = 256;  // threads per block of the loss kernel (nce.cu)
-// 2 doubles of partials per loss block, then one slot holding the check flag.
-constexpr size_t kPartialDoubles = 2 * (kNoAllocMaxEdges / kLossThreads + 1);
-constexpr size_t kScratchDoubles = kPartialDoubles + 32;
+// Two doubles of partials per block of the loss kernel (kNceThreads threads),
+// plus two, as nce_workspace_bytes; then a 16-byte slot holding the check flag.
+constexpr size_t kPartialDoubles = 2 * (kNoAllocMaxEdges / kNceThreads + 1);
+constexpr size_t kScratchDoubles = kPartialDoubles + 2;
+constexpr size_t kScratchBytes = sizeof(double) * kScratchDoubles;
+static_assert(kNoAllocMaxEdges % kNceThreads == 0, "the edge limit fills whole loss blocks");
+static_assert(kScratchBytes == 65568, "the documented size of the scratch array");
 
 __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
-std::mutex g_mu;
-void *g_addr[128] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
+template <class Fn>
+Fn driver_entry(const char *name) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    NCVIS_CUDA(cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q));
+    require(q == cudaDriverEntryPointSuccess && p != nullptr,
+            std::string("nce_loss_noalloc: driver entry point ") + name + " is unavailable",
+            kCudaError);
+    return (Fn)p;
+}
+
+// Unique id of the current context (0 when the thread has none yet).
+unsigned long long current_context_id() {
+    static const CtxGetCurrentFn get_current = driver_entry<CtxGetCurrentFn>("cuCtxGetCurrent");
+    static const CtxGetIdFn get_id = driver_entry<CtxGetIdFn>("cuCtxGetId");
+    CUcontext ctx = nullptr;
+    require(get_current(&ctx) == CUDA_SUCCESS, "nce_loss_noalloc: cuCtxGetCurrent failed",
+            kCudaError);
+    if (!ctx) return 0;
+    unsigned long long id = 0;
+    require(get_id(ctx, &id) == CUDA_SUCCESS, "nce_loss_noalloc: cuCtxGetId failed", kCudaError);
+    return id;
+}
+
+constexpr int kMaxDevices = 128;
+std::mutex g_mu;
+struct Setup {
+    unsigned long long ctx_id = 0;
+    double *addr = nullptr;
+};
+Setup g_setup[kMaxDevices];
+
+// Device address of g_noalloc_scratch on the current device, looked up at
+// set-up (the device's first call, or its first call in a new context).
 double *scratch_on_current_device() {
     int dev = 0;
     NCVIS_CUDA(cudaGetDevice(&dev));
-    require(dev >= 0 && dev < 128, "nce_loss_noalloc: device index out of range");
+    require(dev >= 0 && dev < kMaxDevices, "nce_loss_noalloc: device index out of range");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long id = current_context_id();
+    Setup &e = g_setup[dev];
+    if (id == 0 || e.ctx_id != id || !e.addr) {
         void *p = nullptr;
         NCVIS_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
         require(p != nullptr, "nce_loss_noalloc: no device address for the scratch array",
                 kCudaError);
-        g_addr[dev] = p;
+        e.addr = (double *)p;
+        e.ctx_id = current_context_id();  // the lookup made the context current if it was not
     }
-    return (double *)g_addr[dev];
+    return e.addr;
 }
 
 // flag = 1 if any src/dst entry lies outside [0, N).
@@ -88,6 +133,9 @@ extern "C" int ncvis_nce_loss_device_noalloc(size_t N, size_t d, size_t E, const
                 "nce_loss_noalloc: need 2 <= N < 2^31, 1 <= d <= 32, 1 <= n_noise <= 1024");
         require((int64_t)E <= kNoAllocMaxEdges,
                 "nce_loss_noalloc: at most 2^20 edges per call (E = " + std::to_string(E) + ")");
+        // The loss kernels' partials must stay below the flag slot.
+        require(nce_workspace_bytes((int64_t)E) <= sizeof(double) * kPartialDoubles,
+                "nce_loss_noalloc: the loss workspace exceeds the scratch array", kInternal);
         cudaStream_t s = (cudaStream_t)stream;
         double *scratch = scratch_on_current_device();
         int *flag = (int *)(scratch + kPartialDoubles);
