@@ -4,12 +4,13 @@
 # flags (setup.py:124-126), the brute-force hnswlib stand-in and the pcg-cpp
 # forwarding shim under oracle/shim, plus oracle/ref_driver.cpp.
 #
-# Test infrastructure only: it needs the reference checkout (REF_ROOT,
-# default /root/reference) and pyarrow's vendored pcg-cpp, so it runs where
-# both exist and is skipped elsewhere.  Output goes to oracle/_ref/ only.
+# Test infrastructure only: it needs the reference checkout and pyarrow's
+# vendored pcg-cpp, so it runs where both exist and is skipped elsewhere.  The
+# checkout is NCVIS_REFERENCE_ROOT when set, else a directory named
+# `reference` beside this repository.  Output goes to oracle/_ref/ only.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF_ROOT="${REF_ROOT:-/root/reference}"
+REF_ROOT="${NCVIS_REFERENCE_ROOT:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF_ROOT/src/ncvis.cpp" ]; then
     echo "build_ref: reference sources not found under $REF_ROOT; skipped" >&2
