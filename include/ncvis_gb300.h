@@ -53,6 +53,14 @@ typedef enum ncvis_distance {
 #define NCVIS_KNN_BF16_RERANK 1 /* BF16 tensor-core distances, exact FP32 rerank */
 #define NCVIS_KNN_IVF 2 /* approximate: k-means cells, each searched against its nearest cells
                            with BF16 tensor-core distances, exact FP32 rerank */
+/* Flag, or-ed into knn_precision (or ncvis_knn_device's precision) with
+ * NCVIS_KNN_BF16_RERANK: search the rows in the caller's order.  Without it
+ * the exact BF16 search first orders the rows by k-means cell and sweeps each
+ * query tile's candidates from its own cell onwards (from 32,768 points; the
+ * inner-product spaces, and squared L2 with D <= 126), so that every point's
+ * candidate list is nearly final early; the candidates found are the same up
+ * to exact score ties at the last kept place. */
+#define NCVIS_KNN_CALLER_ORDER 0x100
 
 /* SGD modes (ncvis_options.sgd_mode). */
 #define NCVIS_SGD_HOGWILD 0 /* parallel chains, counter-based noise samples; staged in
@@ -95,6 +103,20 @@ typedef struct ncvis_options {
     int ivf_lists;          /* NCVIS_KNN_IVF: k-means cells; 0: N / 512 (at most 65,536) */
     int ivf_probe;          /* NCVIS_KNN_IVF: cells searched per cell, its own included, at
                                most 64; 0: 32 */
+    long long wait_limit_cycles; /* limit of the tensor-core kNN kernel's waits between its
+                               roles, in SM clock cycles (0: 4e9, about 2 s); a wait that runs
+                               out stops the kernel and the call returns NCVIS_DEVICE_TIMEOUT */
+    int inject_stall;       /* diagnostics: nonzero makes the tensor-core kNN kernel first wait
+                               on a barrier that nothing completes, so that the wait runs out
+                               (a test of the timeout path); 0 in normal use */
+    size_t arena_limit;     /* largest device arena (the fit's device buffers) the engine may
+                               hold, in bytes (0: no limit); a fit that needs more fails as an
+                               allocation failure (NCVIS_CUDA_ERROR) */
+    int init_sequential_stats; /* init_embedding's mean and std: 0 from FP64 partial sums;
+                               nonzero as the reference's one thread sums them (see
+                               ncvis_init_embedding_device) */
+    int knn_order_cells;    /* k-means cells that order the rows before the exact BF16 search
+                               (see NCVIS_KNN_CALLER_ORDER); 0: N / 4096, at least 16 */
 } ncvis_options;
 
 /* Per-stage device times of the last fit_transform, in milliseconds, named
@@ -112,6 +134,8 @@ typedef struct ncvis_stage_times {
     float total_ms;
     int64_t n_edges;     /* symmetrized directed edges E */
     int64_t k;           /* neighbours per point after clamping */
+    float knn_order_ms;  /* part of knn_ms: the k-means cell ordering before the exact BF16
+                            search's sweep (0 when the rows keep the caller's order) */
 } ncvis_stage_times;
 
 typedef struct ncvis_engine *ncvis_handle;
@@ -186,10 +210,14 @@ int ncvis_symmetrize_device(size_t N, size_t k, const int32_t *d_inds, const flo
 
 /* init_embedding over a CSR graph: Y [N, d] ~ U(0,1) from the one-thread
  * pcg64(seed) stream, then n_init_epochs of neighbour averaging with weight
- * alpha followed by per-dimension standardisation. */
+ * alpha followed by per-dimension standardisation.  sequential_stats = 0:
+ * mean and std from FP64 partial sums (the exact statistics rounded once);
+ * nonzero: FP32 sums over the rows in order, as the reference's one thread
+ * forms them (its rounding drifts ~1e-4 relative from the exact statistics at
+ * a million rows; slower, one dependent add chain per dimension). */
 int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
                                 const int32_t *d_cols, uint64_t seed, int n_init_epochs,
-                                float alpha, float *dY, void *stream);
+                                float alpha, int sequential_stats, float *dY, void *stream);
 
 /* Parallel (Hogwild) NCE SGD over epochs [epoch_begin, epoch_end) of an
  * n_epochs schedule; Y and *dQ (device float) updated in place.  n_noise:
@@ -253,10 +281,13 @@ int ncvis_nce_noise_device(size_t N, size_t E, const int32_t *d_src, size_t n_no
  * memory pool already holds all free HBM, a latency-critical loop that must
  * not take the allocator's synchronisation, a framework that forbids
  * allocations outside its own pool).  Same arguments and result.  Its scratch
- * is one fixed 64 KiB device array inside the library (kept on every GPU that
- * loads it until exit), so E <= 2^20 per call; larger E is rejected.  The
- * first call on each device looks up that array's device address; make it
- * before any stream capture.  Calls share the array: calls whose GPU work
+ * is one fixed device array of 65,568 bytes inside the library (kept on every
+ * GPU that loads it until exit), so E <= 2^20 per call; larger E is rejected.
+ * The first call on each device (and the first after that device's context
+ * was re-created) looks up the array's device address and loads the
+ * library's device code there: make it at start-up, while device memory is
+ * free, and before any stream capture.  Each call waits for `stream` (it reads
+ * an argument-check flag back).  Calls share the array: calls whose GPU work
  * overlaps in time race.  No counterpart in the reference (an addition).
  * Errors: ncvis_get_last_error(). */
 int ncvis_nce_loss_device_noalloc(size_t N, size_t d, size_t E, const int32_t *d_src,

@@ -22,6 +22,7 @@ NCVIS_INTERNAL = 5
 KNN_FP32 = 0
 KNN_BF16_RERANK = 1
 KNN_IVF = 2
+KNN_CALLER_ORDER = 0x100  # flag: exact BF16 search in the caller's row order
 SGD_HOGWILD = 0
 SGD_REPLAY = 1
 SGD_HOGWILD_UNSTAGED = 2
@@ -57,6 +58,11 @@ class NcvisOptions(C.Structure):
         ("sgd_chains", C.c_int),
         ("ivf_lists", C.c_int),
         ("ivf_probe", C.c_int),
+        ("wait_limit_cycles", C.c_longlong),
+        ("inject_stall", C.c_int),
+        ("arena_limit", C.c_size_t),
+        ("init_sequential_stats", C.c_int),
+        ("knn_order_cells", C.c_int),
     ]
 
 
@@ -74,6 +80,7 @@ class NcvisStageTimes(C.Structure):
         ("total_ms", C.c_float),
         ("n_edges", C.c_int64),
         ("k", C.c_int64),
+        ("knn_order_ms", C.c_float),
     ]
 
     def as_dict(self) -> dict:
@@ -110,7 +117,7 @@ SIGNATURES = {
     "ncvis_symmetrize_device": (C.c_int, [_sz, _sz, _vp, _vp, _vp, _vp, _vp, _vp,
                                           C.POINTER(_sz), _vp]),
     "ncvis_init_embedding_device": (C.c_int, [_sz, _sz, _vp, _vp, C.c_uint64, C.c_int, C.c_float,
-                                              _vp, _vp]),
+                                              C.c_int, _vp, _vp]),
     "ncvis_optimize_device": (C.c_int, [_sz, _sz, _sz, _vp, _vp, _vp, _vp, C.c_uint64, C.c_int,
                                         C.c_int, C.c_int, C.POINTER(_sz), C.c_float, C.c_float,
                                         C.c_float, C.c_float, C.c_int, _vp]),

@@ -17,7 +17,13 @@ rerank; "ivf" for the approximate search over k-means cells, with
 ``rerank_factor``, ``sgd_mode`` ("hogwild": parallel chains with the
 noise samples staged in shared-memory windows of the embedding where N is
 large enough; "hogwild_unstaged": every noise row read from the whole
-embedding; "replay" with a recorded ``replay_stream``) and ``sgd_chains``.
+embedding; "replay" with a recorded ``replay_stream``) and ``sgd_chains``;
+``knn_order`` (the "bf16" search sweeps rows ordered by k-means cell; False
+keeps the caller's order, same candidates up to exact ties),
+``wait_limit_cycles`` (limit of the tensor-core kernel's waits),
+``arena_limit`` (largest device arena, bytes; 0 = no limit) and
+``init_sequential_stats`` (init's statistics summed as the reference's one
+thread sums them instead of in FP64).
 """
 from __future__ import annotations
 
@@ -82,7 +88,8 @@ class NCVis:
                  random_seed=42, n_epochs=50, n_init_epochs=20, spread=1., min_dist=0.4, a=None,
                  b=None, alpha=1., alpha_Q=1., n_noise=None, distance="euclidean", *,
                  knn_precision="fp32", rerank_factor=0, sgd_mode="hogwild", replay_stream=None,
-                 sgd_chains=0, ivf_lists=0, ivf_probe=0):
+                 sgd_chains=0, ivf_lists=0, ivf_probe=0, knn_order=True, wait_limit_cycles=0,
+                 arena_limit=0, init_sequential_stats=False):
         """Creates a new NCVis instance; arguments as in the reference
         (wrapper/ncvis.pyx:49-101).  M and ef_construction configure HNSW in
         the reference and are accepted and ignored (the kNN here is exact);
@@ -131,6 +138,8 @@ class NCVis:
             raise ValueError("ivf_lists and ivf_probe must be non-negative")
         if int(rerank_factor) < 0 or int(sgd_chains) < 0:
             raise ValueError("rerank_factor and sgd_chains must be non-negative")
+        if int(wait_limit_cycles) < 0 or int(arena_limit) < 0:
+            raise ValueError("wait_limit_cycles and arena_limit must be non-negative")
 
         self.n_epochs = int(n_epochs)
         self.noise_plan = np.ascontiguousarray(negative_plan, dtype=np.uintp)
@@ -144,14 +153,16 @@ class NCVis:
         self._replay = None
         if replay_stream is not None:
             self._replay = np.ascontiguousarray(replay_stream, dtype=np.int32)
+        precision = _PRECISIONS[knn_precision] | (0 if knn_order else _lib.KNN_CALLER_ORDER)
         self._options = _lib.NcvisOptions(
-            knn_precision=_PRECISIONS[knn_precision], rerank_factor=int(rerank_factor),
+            knn_precision=precision, rerank_factor=int(rerank_factor),
             sgd_mode=_SGD_MODES[sgd_mode],
             replay_stream=(self._replay.ctypes.data_as(C.POINTER(C.c_int32))
                            if self._replay is not None else None),
             replay_len=0 if self._replay is None else int(self._replay.size),
             stream=None, sgd_chains=int(sgd_chains), ivf_lists=int(ivf_lists),
-            ivf_probe=int(ivf_probe))
+            ivf_probe=int(ivf_probe), wait_limit_cycles=int(wait_limit_cycles), inject_stall=0,
+            arena_limit=int(arena_limit), init_sequential_stats=int(bool(init_sequential_stats)))
         L = _lib.lib()
         self._h = L.ncvis_create(C.byref(self._params), C.byref(self._options))
         if not self._h:
@@ -166,6 +177,17 @@ class NCVis:
 
     def _set_stream(self, stream_ptr):
         self._options.stream = stream_ptr
+        _lib.check(_lib.lib().ncvis_set_options(self._h, C.byref(self._options)), self._h)
+
+    def set_options(self, **fields):
+        """Changes fields of the engine's options struct (ncvis_options in
+        include/ncvis_gb300.h) for the next calls, e.g. arena_limit or
+        wait_limit_cycles."""
+        for name, value in fields.items():
+            if name not in dict(_lib.NcvisOptions._fields_) or name in ("replay_stream",
+                                                                         "replay_len", "stream"):
+                raise ValueError(f"unknown or fixed option {name!r}")
+            setattr(self._options, name, int(value))
         _lib.check(_lib.lib().ncvis_set_options(self._h, C.byref(self._options)), self._h)
 
     def fit_transform(self, X):

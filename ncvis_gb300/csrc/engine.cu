@@ -243,6 +243,11 @@ struct ncvis_engine {
 
     char *ensure_arena(size_t bytes) {
         if (bytes > arena_bytes) {
+            // A caller-set limit fails the fit as the allocation itself would.
+            if (o.arena_limit && bytes > o.arena_limit)
+                throw Error(kCudaError, "CUDA error out of memory: the device arena needs " +
+                                            std::to_string(bytes) + " bytes, above arena_limit " +
+                                            std::to_string(o.arena_limit));
             if (arena) {
                 NCVIS_CUDA(cudaStreamSynchronize(stream()));
                 NCVIS_CUDA(cudaFree(arena));
@@ -281,11 +286,15 @@ void check_noise(const size_t *n_noise, int begin, int end, const std::string &p
 
 // The options struct as a C caller may fill it: unknown modes and negative
 // counts are refused rather than falling back to a default path.
+int knn_mode(int precision) { return precision & ~NCVIS_KNN_CALLER_ORDER; }
+
 void check_options(const ncvis_options &o) {
-    require(o.knn_precision == NCVIS_KNN_FP32 || o.knn_precision == NCVIS_KNN_BF16_RERANK ||
-                o.knn_precision == NCVIS_KNN_IVF,
+    const int mode = knn_mode(o.knn_precision);
+    require(mode == NCVIS_KNN_FP32 || mode == NCVIS_KNN_BF16_RERANK || mode == NCVIS_KNN_IVF,
             "[ncvis] options: knn_precision must be NCVIS_KNN_FP32, NCVIS_KNN_BF16_RERANK or "
-            "NCVIS_KNN_IVF");
+            "NCVIS_KNN_IVF (optionally with the flag NCVIS_KNN_CALLER_ORDER)");
+    require(o.wait_limit_cycles >= 0, "[ncvis] options: wait_limit_cycles must be non-negative");
+    require(o.knn_order_cells >= 0, "[ncvis] options: knn_order_cells must be non-negative");
     require(o.sgd_mode == NCVIS_SGD_HOGWILD || o.sgd_mode == NCVIS_SGD_REPLAY ||
                 o.sgd_mode == NCVIS_SGD_HOGWILD_UNSTAGED,
             "[ncvis] options: sgd_mode must be NCVIS_SGD_HOGWILD, NCVIS_SGD_REPLAY or "
@@ -345,8 +354,8 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const int k = (int)kk;
     const int d = (int)p.d;
     const int dist = p.distance;
-    const bool ivf = (o.knn_precision == NCVIS_KNN_IVF);
-    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK) || ivf;
+    const bool ivf = (knn_mode(o.knn_precision) == NCVIS_KNN_IVF);
+    const bool bf16 = (knn_mode(o.knn_precision) == NCVIS_KNN_BF16_RERANK) || ivf;
     require((int64_t)N * k < (int64_t(1) << 30), "[ncvis] N * n_neighbors must be below 2^30");
     require(host || ((uintptr_t)Y & (p.d == 4 ? 15 : 7)) == 0,
             "[ncvis] device Y must be 8-byte aligned (16-byte for d = 4)");
@@ -355,12 +364,20 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     cudaStream_t s = stream();
     KnnPlan kp = plan_knn_f32((int64_t)N, k, o.rerank_factor);
     KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, k, o.rerank_factor, dist);
+    tp.wait_cycles = o.wait_limit_cycles;
+    tp.stall = o.inject_stall != 0;
     if (bf16)
         require(knn_tc_supported((int)D, tp.R),
                 "[ncvis] the BF16 tensor-core kNN supports D <= 128", kUnsupported);
     const bool fold = bf16 && tp.fold;
     const int C = bf16 ? tp.R : kp.C();
     const int64_t nk = (int64_t)N * k;
+    // The exact BF16 search with the rows ordered by k-means cell (warm start).
+    const KnnOrderPlan op =
+        (bf16 && !ivf)
+            ? plan_knn_order((int64_t)N, (int)D, tp, dist,
+                             (o.knn_precision & NCVIS_KNN_CALLER_ORDER) ? -1 : o.knn_order_cells)
+            : KnnOrderPlan();
     const int chains = o.sgd_chains > 0 ? o.sgd_chains : 0;  // 0: sized once E is known
 
     Layout L;
@@ -388,6 +405,8 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     const size_t o_init = L.take(init_workspace_bytes((int64_t)N, d));
     const size_t o_sgd = L.take(sgd_workspace_bytes(chains));
     const size_t o_stream = replay ? L.take(sizeof(int32_t) * std::max<size_t>(o.replay_len, 1)) : 0;
+    const size_t ord_bytes = knn_order_workspace_bytes((int64_t)N, (int)D, tp, op);
+    const size_t o_ord = ord_bytes ? L.take(ord_bytes) : 0;
     char *base = ensure_arena(L.total);
 
     const float *dX = (host && !read_host) ? (float *)(base + o_X) : X;
@@ -426,6 +445,9 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         run_knn_ivf(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist,
                     plan_ivf((int64_t)N, o.ivf_lists, o.ivf_probe), (uint64_t)p.random_seed,
                     cand_i, flag + 2, s);
+    else if (op.C > 0)
+        run_knn_tc_ordered(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist, op, (uint64_t)p.random_seed,
+                           cand_i, flag + 2, s, base + o_ord, ord_bytes, ev.ev[9]);
     else if (bf16)
         launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s, nullptr,
                              Xc);
@@ -447,7 +469,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
 
     const float init_alpha = (float)(1. / k);
     run_init_embedding((int64_t)N, d, row_ptr, cols, (uint64_t)p.random_seed, p.n_init_epochs,
-                       init_alpha, dY, base + o_init, s);
+                       init_alpha, dY, base + o_init, s, o.init_sequential_stats != 0);
     NCVIS_CUDA(cudaEventRecord(ev.ev[6], s));
 
     NCVIS_CUDA(cudaMemsetAsync(dQ, 0, sizeof(float), s));
@@ -508,6 +530,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     times.total_ms = ev.ms(0, 8);
     times.n_edges = E;
     times.k = k;
+    times.knn_order_ms = op.C > 0 ? ev.ms(2, 9) : 0.f;
 }
 
 void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets, size_t B,
@@ -530,7 +553,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
             "[ncvis] batched: the replay mode (one recorded noise stream per fit) is not available "
             "for batched problems");
     // Batched problems are small: the IVF mode runs the exact BF16 search here.
-    const bool bf16 = (o.knn_precision == NCVIS_KNN_BF16_RERANK || o.knn_precision == NCVIS_KNN_IVF);
+    const bool bf16 = (knn_mode(o.knn_precision) == NCVIS_KNN_BF16_RERANK ||
+                       knn_mode(o.knn_precision) == NCVIS_KNN_IVF);
     require(((uintptr_t)dY & 7) == 0, "[ncvis] device Y must be 8-byte aligned");
     // k is clamped by the smallest problem (src/ncvis.cpp:381-382 per problem).
     int64_t kk = std::min<int64_t>((int64_t)p.n_neighbors, min_n - 1);
@@ -560,6 +584,8 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
            min_n / (kp.splits * 2) >= 64)
         kp.splits *= 2;
     KnnTcPlan tp = plan_knn_tc(total, (int)D, k, o.rerank_factor, dist);
+    tp.wait_cycles = o.wait_limit_cycles;
+    tp.stall = o.inject_stall != 0;
     const bool fold = bf16 && tp.fold;
     BatchedTcWork tw;
     if (bf16) {
@@ -815,6 +841,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     times.total_ms = ev.ms(0, 8);
     times.n_edges = E;
     times.k = k;
+    times.knn_order_ms = 0.f;
 }
 
 // ------------------------------------------------------------------------ C ABI
@@ -899,11 +926,11 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         require(D >= 1 && N < (size_t(1) << 31) && N * k < (size_t(1) << 30),
                 "knn: need D >= 1, N < 2^31 and N * k < 2^30");
         require(distance >= 0 && distance <= 3, "[ncvis::NCVis::buildKNN] Unrecognized distance type.");
-        require(precision == NCVIS_KNN_FP32 || precision == NCVIS_KNN_BF16_RERANK ||
-                    precision == NCVIS_KNN_IVF,
+        const int mode = knn_mode(precision);
+        require(mode == NCVIS_KNN_FP32 || mode == NCVIS_KNN_BF16_RERANK || mode == NCVIS_KNN_IVF,
                 "knn: unknown precision mode");
-        const bool ivf = (precision == NCVIS_KNN_IVF);
-        const bool bf16 = (precision == NCVIS_KNN_BF16_RERANK) || ivf;
+        const bool ivf = (mode == NCVIS_KNN_IVF);
+        const bool bf16 = (mode == NCVIS_KNN_BF16_RERANK) || ivf;
         cudaStream_t s = (cudaStream_t)stream;
         KnnPlan kp = plan_knn_f32((int64_t)N, (int)k, rerank_factor);
         KnnTcPlan tp = plan_knn_tc((int64_t)N, (int)D, (int)k, rerank_factor, distance);
@@ -912,6 +939,12 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
             require(knn_tc_supported((int)D, tp.R),
                     "knn: the BF16 tensor-core kNN supports D <= 128", kUnsupported);
         const int C = bf16 ? tp.R : kp.C();
+        const KnnOrderPlan op = (bf16 && !ivf) ? plan_knn_order((int64_t)N, (int)D, tp, distance,
+                                                                (precision & NCVIS_KNN_CALLER_ORDER)
+                                                                    ? -1
+                                                                    : 0)
+                                               : KnnOrderPlan();
+        const size_t ord_bytes = knn_order_workspace_bytes((int64_t)N, (int)D, tp, op);
         Layout L;
         const size_t o_Xp = L.take(sizeof(float) * N * D);
         const size_t o_sqn = L.take(sizeof(float) * N);
@@ -920,6 +953,7 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         const size_t o_cd = L.take(sizeof(float) * N * C);
         const size_t o_Xb = bf16 ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
         const size_t o_Xc = fold ? L.take(sizeof(__nv_bfloat16) * N * tp.ldb) : 0;
+        const size_t o_ord = ord_bytes ? L.take(ord_bytes) : 0;
         StreamBuffer buf(L.total, s);
         char *base = (char *)buf.p;
         NCVIS_CUDA(cudaMemsetAsync(base + o_flag, 0, sizeof(int) * 2, s));
@@ -937,6 +971,10 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
             run_knn_ivf((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
                         plan_ivf((int64_t)N, lists, probe), 42, (int32_t *)(base + o_ci),
                         (int *)(base + o_flag) + 1, s);
+        } else if (op.C > 0) {
+            run_knn_tc_ordered((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
+                               op, 42, (int32_t *)(base + o_ci), (int *)(base + o_flag) + 1, s,
+                               base + o_ord, ord_bytes);
         } else if (bf16) {
             launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
                                  (int32_t *)(base + o_ci), (float *)(base + o_cd),
@@ -993,7 +1031,7 @@ int ncvis_symmetrize_device(size_t N, size_t k, const int32_t *d_inds, const flo
 
 int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
                                 const int32_t *d_cols, uint64_t seed, int n_init_epochs,
-                                float alpha, float *dY, void *stream) {
+                                float alpha, int sequential_stats, float *dY, void *stream) {
     return guarded(nullptr, [&] {
         require(d_row_ptr && d_cols && dY, "init_embedding: null pointer");
         require(N >= 1 && d >= 1 && d <= 32 && n_init_epochs >= 0,
@@ -1013,7 +1051,7 @@ int ncvis_init_embedding_device(size_t N, size_t d, const int64_t *d_row_ptr,
                 "init_embedding: a column index is outside [0, N)");
         StreamBuffer ws(init_workspace_bytes((int64_t)N, (int)d), s);
         run_init_embedding((int64_t)N, (int)d, d_row_ptr, d_cols, seed, n_init_epochs, alpha, dY,
-                           ws.p, s);
+                           ws.p, s, sequential_stats != 0);
     });
 }
 

@@ -7,7 +7,9 @@
 //                  (one thread per row, FP32, multiply then add as the
 //                  reference's build does: no fused multiply-add);
 //       mean, population std per dimension (FP64 block partial sums, cast to
-//       FP32 and divided by N in FP32 as the reference does);
+//       FP32 and divided by N in FP32 as the reference does; or, on request,
+//       the reference's one-thread FP32 sums in row order, whose rounding
+//       drifts ~1e-4 relative from the exact statistics at a million rows);
 //       Y_new = (Y_new - mean) / sigma;
 //   ping-pong buffers, result left in Y (src/ncvis.cpp:262-267).
 #include <algorithm>
@@ -171,6 +173,71 @@ __global__ void finish_stat(const double *__restrict__ part, int blocks, int d, 
             stat[c] = (mode == 0) ? v : sqrtf(v);
         }
         __syncthreads();
+    }
+}
+
+// The reference's one-thread statistics (src/ncvis.cpp:226-254 on one
+// thread): per dimension an FP32 sum over the rows in order, mode 0 of the
+// values (stat = sum / N), mode 1 of (y - mean)^2 (stat = sqrt(sum / N)).
+// One block: all threads stage chunks of rows into shared memory with
+// asynchronous copies, the next chunk in flight while lane c < d adds up
+// dimension c of the current one; the adds form one dependent chain per
+// dimension (N FP32 adds, ~2 ms per pass at a million rows).
+constexpr int kSeqFloats = 8192;  // floats per staged chunk (32 KB; whole rows)
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads) sequential_stat(const float *__restrict__ Y, int64_t N,
+                                                            int d, int mode,
+                                                            const float *__restrict__ mean,
+                                                            float *__restrict__ stat) {
+    extern __shared__ float chunk[];  // [2][rows_per * d]
+    const int64_t rows_per = kSeqFloats / d;
+    const int64_t per = rows_per * d;
+    const int64_t n = N * d;
+    const int64_t chunks = (n + per - 1) / per;
+    auto issue = [&](int64_t k) {
+        float *dst = chunk + (k & 1) * per;
+        const int64_t base = k * per;
+        const int64_t len = min(per, n - base);
+        for (int64_t t = threadIdx.x; t < len; t += blockDim.x) cp_async4(dst + t, Y + base + t);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    const int c = threadIdx.x;
+    const float m = (mode == 1 && c < d) ? mean[c] : 0.f;
+    float s = 0.f;
+    issue(0);
+    for (int64_t k = 0; k < chunks; ++k) {
+        if (k + 1 < chunks) {
+            issue(k + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        if (c < d) {
+            const float *v = chunk + (k & 1) * per;
+            const int64_t rows = min(rows_per, N - k * rows_per);
+#pragma unroll 8
+            for (int64_t r = 0; r < rows; ++r) {
+                float t = v[r * d + c];
+                if (mode == 1) {
+                    t = __fsub_rn(t, m);
+                    t = __fmul_rn(t, t);
+                }
+                s = __fadd_rn(s, t);
+            }
+        }
+        __syncthreads();
+    }
+    if (c < d) {
+        const float v = __fdiv_rn(s, (float)N);
+        stat[c] = (mode == 0) ? v : __fsqrt_rn(v);
     }
 }
 
@@ -374,8 +441,13 @@ size_t init_workspace_bytes(int64_t N, int d) {
 
 void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t *cols,
                         uint64_t seed, int n_init_epochs, float alpha, float *Y, void *workspace,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool sequential_stats) {
     require(d >= 1 && d <= kMaxDim, "init_embedding: d must be in [1, 32]");
+    const size_t seq_smem = sizeof(float) * 2 * (size_t)(kSeqFloats / d) * d;
+    if (sequential_stats)
+        NCVIS_CUDA(cudaFuncSetAttribute(sequential_stat,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)seq_smem));
     const int64_t blocks = (N + kThreads - 1) / kThreads;
     char *p = (char *)workspace;
     float *other = (float *)p;   p += align256(sizeof(float) * N * d);
@@ -414,9 +486,16 @@ void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t 
                 NCVIS_LAUNCH(spmm_rows, (unsigned)blocks, kThreads, 0, s, N, d, row_ptr, cols,
                              alpha, y_old, y_new, part);
         }
-        NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 0, mean);
-        NCVIS_LAUNCH(centred_squares, (unsigned)blocks, kThreads, 0, s, N, d, y_new, mean, part);
-        NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 1, sigma);
+        if (sequential_stats) {
+            NCVIS_LAUNCH(sequential_stat, 1, kThreads, seq_smem, s, y_new, N, d, 0, nullptr,
+                         mean);
+            NCVIS_LAUNCH(sequential_stat, 1, kThreads, seq_smem, s, y_new, N, d, 1, mean, sigma);
+        } else {
+            NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 0, mean);
+            NCVIS_LAUNCH(centred_squares, (unsigned)blocks, kThreads, 0, s, N, d, y_new, mean,
+                         part);
+            NCVIS_LAUNCH(finish_stat, 1, 1024, 0, s, part, (int)blocks, d, N, 1, sigma);
+        }
         NCVIS_LAUNCH(standardize, elem_grid, kThreads, 0, s, n, d, y_new, mean, sigma);
     }
     if (n_init_epochs % 2)

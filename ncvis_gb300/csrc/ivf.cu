@@ -1,5 +1,7 @@
 // K10: approximate kNN candidate selection by an inverted-file partition, for
-// point counts where the exact O(N^2 D) selection of K2 stops being viable.
+// point counts where the exact O(N^2 D) selection of K2 stops being viable;
+// and the exact selection's warm start, which orders the rows by the same
+// k-means cells (end of this file).
 // The reference's own kNN (hnswlib, src/ncvis.cpp:72-153) is approximate too;
 // its result contract is kept: the candidates found here go through the same
 // exact FP32 rerank (K4), so rows hold k+1 nearest-found points, the nearest
@@ -120,6 +122,33 @@ __global__ void ivf_update(float *__restrict__ cent, float *__restrict__ sums,
     if (lane == 0) counts[c] = 0;
 }
 
+// The same with per-block sums in shared memory (C * D floats and C counts),
+// flushed to the global sums once per block: same-cell updates meet in the
+// SM instead of the L2.
+__global__ void ivf_accumulate_shared(const float *__restrict__ Xp, int64_t N, int D,
+                                      const int32_t *__restrict__ cand, int R, int C,
+                                      float *__restrict__ sums, int *__restrict__ counts) {
+    extern __shared__ float sh[];
+    float *ssum = sh;
+    int *scnt = reinterpret_cast<int *>(sh + (size_t)C * D);
+    for (int t = threadIdx.x; t < C * D; t += blockDim.x) ssum[t] = 0.f;
+    for (int t = threadIdx.x; t < C; t += blockDim.x) scnt[t] = 0;
+    __syncthreads();
+    const int warps = blockDim.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t i = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5); i < N;
+         i += (int64_t)gridDim.x * warps) {
+        const int c = cand[i * R];
+        if (c < 0 || c >= C) continue;
+        for (int t = lane; t < D; t += 32) atomicAdd(ssum + c * D + t, Xp[i * D + t]);
+        if (lane == 0) atomicAdd(scnt + c, 1);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < C * D; t += blockDim.x)
+        if (ssum[t] != 0.f) atomicAdd(sums + t, ssum[t]);
+    for (int t = threadIdx.x; t < C; t += blockDim.x)
+        if (scnt[t]) atomicAdd(counts + t, scnt[t]);
+}
+
 __global__ void ivf_count(const int32_t *__restrict__ cand, int R, int64_t N, int C,
                           int *__restrict__ counts) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -172,12 +201,17 @@ HostWork all_pairs_work(int64_t nq, int64_t nc) {
     return w;
 }
 
-// Stream-ordered device allocations freed when the owner goes out of scope
-// (on every exit path, errors included).
+// Device buffers of one call: carved from the caller's workspace when one is
+// given (256-byte aligned, bounded by its size), else stream-ordered
+// allocations freed when the owner goes out of scope (on every exit path,
+// errors included).
 struct DeviceArena {
     cudaStream_t s;
+    char *base = nullptr;
+    size_t cap = 0, used = 0;
     std::vector<void *> ptrs;
-    explicit DeviceArena(cudaStream_t st) : s(st) {}
+    explicit DeviceArena(cudaStream_t st, void *workspace = nullptr, size_t bytes = 0)
+        : s(st), base((char *)workspace), cap(bytes) {}
     DeviceArena(const DeviceArena &) = delete;
     DeviceArena &operator=(const DeviceArena &) = delete;
     ~DeviceArena() {
@@ -185,8 +219,16 @@ struct DeviceArena {
     }
     template <typename T>
     T *alloc(size_t count) {
+        const size_t bytes = (sizeof(T) * std::max<size_t>(count, 1) + 255) & ~(size_t)255;
+        if (base) {
+            require(used + bytes <= cap, "knn: workspace too small for the cell ordering",
+                    kInternal);
+            T *p = (T *)(base + used);
+            used += bytes;
+            return p;
+        }
         void *p = nullptr;
-        NCVIS_CUDA(cudaMallocAsync(&p, sizeof(T) * std::max<size_t>(count, 1), s));
+        NCVIS_CUDA(cudaMallocAsync(&p, bytes, s));
         ptrs.push_back(p);
         return (T *)p;
     }
@@ -208,8 +250,104 @@ void check_timeout(int *flag, cudaStream_t s) {
     int timeout = 0;
     NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     NCVIS_CUDA(cudaStreamSynchronize(s));
-    require(timeout == 0, "knn (ivf): the tensor-core kernel timed out waiting on a barrier",
+    require(timeout == 0, "knn: the tensor-core kernel timed out waiting on a barrier",
             kDeviceTimeout);
+}
+
+// k-means cells of the points and the points sorted by cell.
+struct Cells {
+    int C = 0;
+    __nv_bfloat16 *Cq = nullptr, *Cc = nullptr;  // centroid rows: query side, candidate side
+    std::vector<int> counts;                     // points per cell (host)
+    std::vector<int64_t> starts;                 // C + 1 offsets of the cells (host)
+    int32_t *perm = nullptr;                     // sorted position -> original row
+    __nv_bfloat16 *Xs = nullptr, *Xcs = nullptr;  // rows (and folded candidate rows) in cell order
+};
+
+// Step 1: `iters` k-means moves of C centroids (initial centroids: rows drawn
+// with Philox from `seed`), each after an assignment by the tensor-core
+// selection kernel, and a final assignment: point i's cell is cand[i * 32].
+// Centroids are unit length for cosine and correlation.
+void kmeans_cells(const float *Xp, const __nv_bfloat16 *Xb, int64_t N, int D,
+                  const KnnTcPlan &tp, int dist, int C, int iters, uint64_t seed, int32_t *cand,
+                  int *timeout_flag, cudaStream_t s, DeviceArena &arena, Cells &cells) {
+    const bool fold = tp.fold;
+    const int ldb = tp.ldb;
+    cells.C = C;
+    float *cent = arena.alloc<float>((size_t)C * D);
+    float *sums = arena.alloc<float>((size_t)C * D);
+    int *counts = arena.alloc<int>(C);
+    cells.Cq = arena.alloc<__nv_bfloat16>((size_t)C * ldb);
+    cells.Cc = fold ? arena.alloc<__nv_bfloat16>((size_t)C * ldb) : cells.Cq;
+    uint32_t k0, k1;
+    noise_key(seed ^ 0x1f51f51full, k0, k1);
+    const unsigned warps_c = ceil_div((size_t)C, 8);
+    NCVIS_LAUNCH(ivf_init, warps_c, 256, 0, s, Xp, N, D, C, k0, k1, cent);
+    NCVIS_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * C * D, s));
+    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
+    KnnTcPlan ap = tp;
+    ap.R = 32;
+    const TcWork awork = upload(all_pairs_work(N, C), nullptr, arena);
+    const int normalise = (dist == kCosine || dist == kCorrelation) ? 1 : 0;
+    // Per-block sums in shared memory where C * D floats fit in 110 KB (two
+    // blocks per SM), else straight into the global sums.
+    const size_t acc_smem = sizeof(float) * (size_t)C * D + sizeof(int) * (size_t)C;
+    const bool shared_acc = acc_smem <= 110 * 1024;
+    if (shared_acc)
+        NCVIS_CUDA(cudaFuncSetAttribute(ivf_accumulate_shared,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)acc_smem));
+    for (int pass = 0;; ++pass) {
+        NCVIS_LAUNCH(ivf_centroid_rows, warps_c, 256, 0, s, cent, C, D, ldb, fold ? 1 : 0,
+                     cells.Cq, fold ? cells.Cc : cells.Cq);
+        launch_knn_select_tc_pair(Xb, N, cells.Cc, C, nullptr, ap, true, cand, timeout_flag, s,
+                                  awork);
+        if (pass == iters) break;
+        if (shared_acc)
+            NCVIS_LAUNCH(ivf_accumulate_shared, (unsigned)(2 * num_sms()), 512, acc_smem, s, Xp,
+                         N, D, cand, 32, C, sums, counts);
+        else
+            NCVIS_LAUNCH(ivf_accumulate, (unsigned)ceil_div((size_t)N, 8), 256, 0, s, Xp, N, D,
+                         cand, 32, C, sums, counts);
+        NCVIS_LAUNCH(ivf_update, warps_c, 256, 0, s, cent, sums, counts, C, D, normalise);
+    }
+}
+
+// Step 2: counting sort of the points by cell (within a cell, the order in
+// which the scatter's atomics arrive) and their BF16 rows gathered in that
+// order; waits on the stream for the cell sizes.
+void sort_by_cell(const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc, int64_t N, int ldb,
+                  const int32_t *cand, int *timeout_flag, cudaStream_t s, DeviceArena &arena,
+                  Cells &cells) {
+    const int C = cells.C;
+    int *counts = arena.alloc<int>(C);
+    int *cursor = arena.alloc<int>(C);
+    int64_t *d_starts = arena.alloc<int64_t>((size_t)C + 1);
+    cells.perm = arena.alloc<int32_t>((size_t)N);
+    cells.Xs = arena.alloc<__nv_bfloat16>((size_t)N * ldb);
+    cells.Xcs = Xc ? arena.alloc<__nv_bfloat16>((size_t)N * ldb) : nullptr;
+    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
+    NCVIS_LAUNCH(ivf_count, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, 32, N, C,
+                 counts);
+    cells.counts.assign(C, 0);
+    NCVIS_CUDA(cudaMemcpyAsync(cells.counts.data(), counts, sizeof(int) * C,
+                               cudaMemcpyDeviceToHost, s));
+    NCVIS_CUDA(cudaStreamSynchronize(s));
+    check_timeout(timeout_flag, s);
+    cells.starts.assign(C + 1, 0);
+    for (int c = 0; c < C; ++c) cells.starts[c + 1] = cells.starts[c] + cells.counts[c];
+    require(cells.starts[C] == N, "knn: a point was not assigned to a cell", kInternal);
+    NCVIS_CUDA(cudaMemcpyAsync(d_starts, cells.starts.data(), sizeof(int64_t) * (C + 1),
+                               cudaMemcpyHostToDevice, s));
+    NCVIS_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * C, s));
+    NCVIS_LAUNCH(ivf_scatter, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, 32, N, C,
+                 d_starts, cursor, cells.perm);
+    const size_t vec = (size_t)N * (ldb / 8);
+    NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xb, cells.perm, N, ldb,
+                 cells.Xs);
+    if (Xc)
+        NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xc, cells.perm, N,
+                     ldb, cells.Xcs);
 }
 
 }  // namespace
@@ -231,76 +369,29 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
             "knn (ivf): squared L2 needs D <= 126 (the folded-norm product)", kUnsupported);
     require(N < (int64_t(1) << 31), "knn (ivf): N must be below 2^31");
     const bool fold = tp.fold;
-    const int C = ip.C, ldb = tp.ldb;
+    const int C = ip.C;
     const int Rp = ip.probe > 32 ? 64 : 32;  // nearest cells listed per cell
     DeviceArena arena(s);
-    float *cent = arena.alloc<float>((size_t)C * D);
-    float *sums = arena.alloc<float>((size_t)C * D);
-    int *counts = arena.alloc<int>(C);
-    int *cursor = arena.alloc<int>(C);
-    __nv_bfloat16 *Cq = arena.alloc<__nv_bfloat16>((size_t)C * ldb);
-    __nv_bfloat16 *Cc = fold ? arena.alloc<__nv_bfloat16>((size_t)C * ldb) : nullptr;
-    int32_t *pcand = arena.alloc<int32_t>((size_t)C * Rp);
-    int32_t *perm = arena.alloc<int32_t>((size_t)N);
-    int64_t *d_starts = arena.alloc<int64_t>((size_t)C + 1);
-    __nv_bfloat16 *Xs = arena.alloc<__nv_bfloat16>((size_t)N * ldb);
-    __nv_bfloat16 *Xcs = fold ? arena.alloc<__nv_bfloat16>((size_t)N * ldb) : nullptr;
-    const __nv_bfloat16 *Ccand = fold ? Cc : Cq;
-
-    // 1. k-means: ip.iters moves of the centroids, each after an assignment.
-    uint32_t k0, k1;
-    noise_key(seed ^ 0x1f51f51full, k0, k1);
-    const unsigned warps_c = ceil_div((size_t)C, 8);
-    NCVIS_LAUNCH(ivf_init, warps_c, 256, 0, s, Xp, N, D, C, k0, k1, cent);
-    NCVIS_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * C * D, s));
-    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
-    KnnTcPlan ap = tp;
-    ap.R = 32;
-    const TcWork awork = upload(all_pairs_work(N, C), nullptr, arena);
-    const int normalise = (dist == kCosine || dist == kCorrelation) ? 1 : 0;
-    for (int pass = 0;; ++pass) {
-        NCVIS_LAUNCH(ivf_centroid_rows, warps_c, 256, 0, s, cent, C, D, ldb, fold ? 1 : 0, Cq,
-                     fold ? Cc : Cq);
-        launch_knn_select_tc_pair(Xb, N, Ccand, C, nullptr, ap, true, cand_i, timeout_flag, s,
-                                  awork);
-        if (pass == ip.iters) break;
-        NCVIS_LAUNCH(ivf_accumulate, (unsigned)ceil_div((size_t)N, 8), 256, 0, s, Xp, N, D, cand_i,
-                     32, C, sums, counts);
-        NCVIS_LAUNCH(ivf_update, warps_c, 256, 0, s, cent, sums, counts, C, D, normalise);
-    }
-    check_timeout(timeout_flag, s);
+    Cells cells;
+    // 1. k-means.
+    kmeans_cells(Xp, Xb, N, D, tp, dist, C, ip.iters, seed, cand_i, timeout_flag, s, arena, cells);
 
     // Nearest cells of each cell (its own first for the spaces where a
     // centroid is its own best match; the work list adds it where not).
+    int32_t *pcand = arena.alloc<int32_t>((size_t)C * Rp);
     KnnTcPlan pp = tp;
     pp.R = Rp;
-    launch_knn_select_tc_pair(Cq, C, Ccand, C, nullptr, pp, true, pcand, timeout_flag, s,
+    launch_knn_select_tc_pair(cells.Cq, C, cells.Cc, C, nullptr, pp, true, pcand, timeout_flag, s,
                               upload(all_pairs_work(C, C), nullptr, arena));
 
     // 2. Counting sort by cell.
-    NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
-    NCVIS_LAUNCH(ivf_count, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand_i, 32, N, C,
-                 counts);
-    std::vector<int> h_counts(C);
+    sort_by_cell(Xb, fold ? Xc : nullptr, N, tp.ldb, cand_i, timeout_flag, s, arena, cells);
     std::vector<int32_t> h_pcand((size_t)C * Rp);
-    NCVIS_CUDA(cudaMemcpyAsync(h_counts.data(), counts, sizeof(int) * C, cudaMemcpyDeviceToHost, s));
     NCVIS_CUDA(cudaMemcpyAsync(h_pcand.data(), pcand, sizeof(int32_t) * C * Rp,
                                cudaMemcpyDeviceToHost, s));
     NCVIS_CUDA(cudaStreamSynchronize(s));
-    check_timeout(timeout_flag, s);
-    std::vector<int64_t> starts(C + 1, 0);
-    for (int c = 0; c < C; ++c) starts[c + 1] = starts[c] + h_counts[c];
-    require(starts[C] == N, "knn (ivf): a point was not assigned to a cell", kInternal);
-    NCVIS_CUDA(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * (C + 1),
-                               cudaMemcpyHostToDevice, s));
-    NCVIS_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * C, s));
-    NCVIS_LAUNCH(ivf_scatter, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand_i, 32, N, C,
-                 d_starts, cursor, perm);
-    const size_t vec = (size_t)N * (ldb / 8);
-    NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xb, perm, N, ldb, Xs);
-    if (fold)
-        NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xc, perm, N, ldb,
-                     Xcs);
+    const std::vector<int> &h_counts = cells.counts;
+    const std::vector<int64_t> &starts = cells.starts;
 
     // 3. Work list: every 256-row query tile of a cell, one item per probed cell.
     struct Tile {
@@ -358,8 +449,101 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
     }
 
     // 4. The search over the sorted rows, written in original numbering.
-    launch_knn_select_tc_pair(Xs, N, fold ? Xcs : Xs, N, nullptr, tp, true, cand_i, timeout_flag,
-                              s, upload(sw, perm, arena));
+    launch_knn_select_tc_pair(cells.Xs, N, fold ? cells.Xcs : cells.Xs, N, nullptr, tp, true,
+                              cand_i, timeout_flag, s, upload(sw, cells.perm, arena));
+    check_timeout(timeout_flag, s);
+}
+
+// ---- warm start of the exact selection ---------------------------------------
+// The exact search keeps each point's best R candidates in a sorted list and
+// inserts a candidate only when it beats the list's worst; with the rows in
+// the caller's order the lists tighten slowly (a sweep over N random
+// candidates inserts ~R ln(N/R) of them per point), and every insertion costs
+// the selection kernel a divergent append path.  Here the rows are ordered by
+// k-means cell and every 256-row query tile sweeps the candidates starting at
+// its own cell (then on to the end and around from row 0): every candidate
+// tile is still scanned exactly once, so the result is the exact search's
+// (the same candidate sets, up to exact score ties at the R-th place), but
+// each point meets its own cell first and its list is nearly final after it.
+// Consecutive query tiles go to consecutive CTAs, so the CTAs running at one
+// time start at nearby rows and share their candidate tiles in the L2.
+
+KnnOrderPlan plan_knn_order(int64_t N, int D, const KnnTcPlan &tp, int dist, int cells) {
+    KnnOrderPlan p;
+    if (cells < 0) return p;
+    // The folded squared-L2 product or an inner-product space (the
+    // assignment ranks centroids by the product); D > 126 squared L2 keeps
+    // the caller's order.
+    if (!(tp.fold || dist != kSquaredL2) || N < kKnnOrderMinRows) return p;
+    int64_t c = cells > 0 ? cells : N / 4096;
+    c = std::max<int64_t>(16, std::min<int64_t>({c, N / 256, 4096}));
+    p.C = (int)c;
+    p.iters = 3;
+    (void)D;
+    return p;
+}
+
+size_t knn_order_workspace_bytes(int64_t N, int D, const KnnTcPlan &tp, const KnnOrderPlan &op) {
+    if (op.C <= 0) return 0;
+    auto a = [](size_t b) { return (std::max<size_t>(b, 1) + 255) & ~(size_t)255; };
+    const size_t C = (size_t)op.C, ldb = (size_t)tp.ldb, n = (size_t)N;
+    const size_t tiles = (n + 255) / 256, ctas = 1024;  // work-list bounds (ctas <= SMs)
+    size_t b = 0;
+    // kmeans_cells: centroids, sums, counts, centroid rows, the assignment work list.
+    b += 2 * a(sizeof(float) * C * D) + a(sizeof(int) * C) + 2 * a(2 * C * ldb);
+    b += a(sizeof(int64_t) * (ctas + 1)) + a(sizeof(TcItem) * tiles);
+    // sort_by_cell: counts, cursors, starts, permutation, sorted rows.
+    b += 2 * a(sizeof(int) * C) + a(sizeof(int64_t) * (C + 1)) + a(sizeof(int32_t) * n);
+    b += 2 * a(2 * n * ldb);
+    // the sweep's work list.
+    b += a(sizeof(int64_t) * (ctas + 1)) + a(sizeof(TcItem) * 2 * tiles);
+    return b;
+}
+
+void run_knn_tc_ordered(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc,
+                        int64_t N, int D, const KnnTcPlan &tp, int dist, const KnnOrderPlan &op,
+                        uint64_t seed, int32_t *cand_i, int *timeout_flag, cudaStream_t s,
+                        void *workspace, size_t workspace_bytes, cudaEvent_t sweep_start) {
+    require(op.C > 0, "knn: ordered search without cells", kInternal);
+    require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
+    require(num_sms() <= 1024, "knn: more SMs than the ordered search's work list allows",
+            kUnsupported);
+    const bool fold = tp.fold;
+    DeviceArena arena(s, workspace, workspace_bytes);
+    Cells cells;
+    kmeans_cells(Xp, Xb, N, D, tp, dist, op.C, op.iters, seed, cand_i, timeout_flag, s, arena,
+                 cells);
+    sort_by_cell(Xb, fold ? Xc : nullptr, N, tp.ldb, cand_i, timeout_flag, s, arena, cells);
+
+    // Work list: query tile t of the sorted rows against [s0, N) then [0, s0),
+    // s0 = its first row's cell start rounded down to a candidate tile; tile t
+    // goes to CTA t mod ctas.
+    const int64_t tiles = (N + 255) / 256;
+    HostWork w;
+    w.ctas = (int)std::min<int64_t>(tiles, num_sms());
+    std::vector<std::vector<TcItem>> per(w.ctas);
+    int c = 0;
+    for (int64_t t = 0; t < tiles; ++t) {
+        const int64_t r0 = 256 * t;
+        while (cells.starts[c + 1] <= r0) ++c;
+        const int64_t s0 = cells.starts[c] / 128 * 128;
+        std::vector<TcItem> &v = per[t % w.ctas];
+        if (s0 == 0) {
+            v.push_back(TcItem{(int)r0, (int)N, 0, (int)N, 0, 0, 0, 0});
+        } else {
+            v.push_back(TcItem{(int)r0, (int)N, (int)s0, (int)N, 0, kTcMore, 0, 0});
+            v.push_back(TcItem{(int)r0, (int)N, 0, (int)s0, 0, kTcContinue, 0, 0});
+        }
+    }
+    w.begin.assign(w.ctas + 1, 0);
+    for (int b = 0; b < w.ctas; ++b) {
+        w.items.insert(w.items.end(), per[b].begin(), per[b].end());
+        w.begin[b + 1] = (int64_t)w.items.size();
+    }
+    const TcWork sweep = upload(w, cells.perm, arena);
+    if (sweep_start) NCVIS_CUDA(cudaEventRecord(sweep_start, s));
+    launch_knn_select_tc_pair(cells.Xs, N, fold ? cells.Xcs : cells.Xs, N, nullptr, tp, true,
+                              cand_i, timeout_flag, s, sweep);
     check_timeout(timeout_flag, s);
 }
 

@@ -32,6 +32,11 @@
 //     inner-product one (otherwise the scan adds the FP32 norms per column).
 // Every mbarrier wait is bounded in time: on expiry the CTA sets *err,
 // stops, drains its MMAs and in-flight TMA copies, frees TMEM and returns.
+// The waits between roles use the plan's limit (default ~2 s); the drain
+// waits always use the long one.  An epilogue warp decides as a warp (votes)
+// whether to stop, so its lanes never part at a warp-collective instruction.
+// A diagnostic stall makes the producer first wait on a barrier that nothing
+// completes, so that the timeout path runs deterministically.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -71,6 +76,7 @@ struct SharedStorage {
     uint64_t a_full, a_empty;
     uint64_t acc_full[2][2], acc_empty[2][2];  // [buffer][query half]
     uint64_t drain;
+    uint64_t never;  // completed by nothing: the diagnostic stall waits on it
     uint32_t tmem_base;
     volatile int abort;
 };
@@ -105,13 +111,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase of `parity`; false if it expired or the CTA aborted.
+// Bounded wait (`limit` SM cycles) for the phase of `parity`; false if it
+// expired or the CTA aborted.
 __device__ __forceinline__ bool mbar_wait(SharedStorage &s, uint64_t *bar, uint32_t parity,
-                                          int *err, int code) {
+                                          int *err, int code, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (s.abort) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             s.abort = 1;
             atomicExch(err, code);
             return false;
@@ -317,7 +324,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                   const __grid_constant__ CUtensorMap tmap_c, const float *__restrict__ sqnorm,
                   int64_t N, int ksteps, int katoms, const int64_t *__restrict__ work_begin,
                   const TcItem *__restrict__ work, const int32_t *__restrict__ row_map,
-                  int32_t *__restrict__ cand_i, int *__restrict__ err) {
+                  int32_t *__restrict__ cand_i, int *__restrict__ err, long long wait_limit,
+                  int stall) {
     extern __shared__ uint8_t smem_raw[];
     SharedStorage &s = *reinterpret_cast<SharedStorage *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -343,6 +351,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 mbar_init(&s.acc_empty[i][hh], kEpiWarps / 2);
             }
         mbar_init(&s.drain, 2);
+        mbar_init(&s.never, 1);
         s.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -367,10 +376,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int i = 0; i < kStages; ++i) issued[i] = false, issued_parity[i] = 0;
         bool a_issued = false;
         uint32_t a_parity = 0;
+        if (stall) mbar_wait(s, &s.never, 0, err, 7, wait_limit);
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
             const QueryTile q = work_item(work_begin, work, it, N);
             if (!q.cont) {
-                if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1)) break;
+                if (!mbar_wait(s, &s.a_empty, a_phase ^ 1, err, 1, wait_limit)) break;
                 mbar_expect_tx(&s.a_full, a_bytes);
                 for (int h = 0; h < 2; ++h)
                     for (int at = 0; at < katoms; ++at)
@@ -381,7 +391,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 a_phase ^= 1;
             }
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
-                if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2)) break;
+                if (!mbar_wait(s, &s.empty[stage], phase ^ 1, err, 2, wait_limit)) break;
                 mbar_expect_tx(&s.full[stage], b_bytes);
                 for (int at = 0; at < katoms; ++at)
                     tma_load_2d(s.b[stage][at], &tmap_c, &s.full[stage], at * 64,
@@ -411,13 +421,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int64_t it = 0; it < n_items && !s.abort; ++it) {
             const QueryTile q = work_item(work_begin, work, it, N);
             if (!q.cont) {
-                if (!mbar_wait(s, &s.a_full, a_phase, err, 3)) break;
+                if (!mbar_wait(s, &s.a_full, a_phase, err, 3, wait_limit)) break;
                 a_phase ^= 1;
             }
             tmem_fence_after();
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
-                if (!mbar_wait(s, &s.acc_empty[acc][h], acc_phase ^ 1, err, 4)) break;
-                if (!mbar_wait(s, &s.full[stage], phase, err, 5)) break;
+                if (!mbar_wait(s, &s.acc_empty[acc][h], acc_phase ^ 1, err, 4, wait_limit)) break;
+                if (!mbar_wait(s, &s.full[stage], phase, err, 5, wait_limit)) break;
                 tmem_fence_after();
                 {
                     const uint32_t d_tmem = tmem + (uint32_t)(acc * 256 + h * 128);
@@ -457,7 +467,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         int32_t li[R];
         float worst = FLT_MAX;
         int qlen = 0;
-        for (int64_t it = 0; it < n_items && !s.abort; ++it) {
+        for (int64_t it = 0; it < n_items; ++it) {
+            // Lanes read the abort flag at different times: the warp stops as one.
+            if (__any_sync(0xffffffffu, s.abort != 0)) break;
             const QueryTile q = work_item(work_begin, work, it, N);
             const int64_t grow = q.row0 + row_in_tile;
             const bool live = grow < q.qend;
@@ -472,7 +484,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             bool ok = true;
             for (int64_t ct = q.lo / kCandTile; ct * kCandTile < q.hi; ++ct) {
-                if (!mbar_wait(s, &s.acc_full[acc][h], acc_phase, err, 6)) {
+                const bool got = mbar_wait(s, &s.acc_full[acc][h], acc_phase, err, 6, wait_limit);
+                if (!__all_sync(0xffffffffu, got)) {
                     ok = false;
                     break;
                 }
@@ -659,7 +672,8 @@ void launch_select(const CUtensorMap &map, const CUtensorMap &map_c, const float
         NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
         NCVIS_LAUNCH(kernel, grid, kThreads, smem, s, map, map_c, sqnorm, N, ksteps, katoms,
-                     work_begin, items, row_map, cand_i, timeout_flag);
+                     work_begin, items, row_map, cand_i, timeout_flag,
+                     plan.wait_cycles > 0 ? plan.wait_cycles : kWaitCycles, plan.stall ? 1 : 0);
     };
     if (plan.R == 32)
         ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);

@@ -54,6 +54,11 @@ struct KnnTcPlan {
     int ldb;     // padded row length of Xb (bf16 elements)
     bool fold;   // squared L2 with the norms folded into the product (needs Xc)
     int64_t Npad;
+    // Diagnostics: limit of the kernel's waits between its roles in SM cycles
+    // (<= 0: about 2 s), and a stall on a barrier nothing completes (the
+    // timeout path's test).
+    long long wait_cycles = 0;
+    bool stall = false;
 };
 KnnTcPlan plan_knn_tc(int64_t N, int D, int k, int rerank_factor, int dist);
 bool knn_tc_supported(int D, int R);
@@ -94,6 +99,27 @@ void run_knn_ivf(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *
                  int D, const KnnTcPlan &tp, int dist, const IvfPlan &ip, uint64_t seed,
                  int32_t *cand_i, int *timeout_flag, cudaStream_t s);
 
+// The exact selection with the rows ordered by k-means cell, each query
+// tile's sweep starting at its own cell (warm start; same candidates as
+// launch_knn_select_tc up to exact score ties at the R-th place).  Applies
+// to the inner-product spaces and the folded squared-L2 product, from
+// kKnnOrderMinRows points; C == 0 means the caller's order.
+constexpr int64_t kKnnOrderMinRows = 32768;
+struct KnnOrderPlan {
+    int C = 0, iters = 0;
+};
+// cells: 0 automatic (N / 4096, at least 16), -1 never, > 0 that many.
+KnnOrderPlan plan_knn_order(int64_t N, int D, const KnnTcPlan &tp, int dist, int cells);
+// Workspace of run_knn_tc_ordered (0 when op.C == 0).  With workspace ==
+// nullptr the call allocates stream-ordered memory instead.  Waits on the
+// stream (cell sizes, timeout flag).
+size_t knn_order_workspace_bytes(int64_t N, int D, const KnnTcPlan &tp, const KnnOrderPlan &op);
+void run_knn_tc_ordered(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc,
+                        int64_t N, int D, const KnnTcPlan &tp, int dist, const KnnOrderPlan &op,
+                        uint64_t seed, int32_t *cand_i, int *timeout_flag, cudaStream_t s,
+                        void *workspace = nullptr, size_t workspace_bytes = 0,
+                        cudaEvent_t sweep_start = nullptr);
+
 // Queries from Q (nq rows) against candidates from Cm (nc rows), both bf16
 // [rows, plan.ldb]; c_sqnorm: candidate squared norms (used for squared L2
 // without the folded norms); `ip`: rank by the product (inner-product spaces,
@@ -122,9 +148,12 @@ void launch_exclusive_scan_i32_to_i64(const int32_t *in, int64_t *out, int64_t n
 
 // ---- K6 init (src/ncvis.cpp:184-273) ------------------------------------------
 size_t init_workspace_bytes(int64_t N, int d);
+// sequential_stats: the per-dimension mean and std as the reference's one
+// thread sums them (FP32, rows in order; slower: one dependent add chain per
+// dimension) instead of FP64 partial sums.
 void run_init_embedding(int64_t N, int d, const int64_t *row_ptr, const int32_t *cols,
                         uint64_t seed, int n_init_epochs, float alpha, float *Y, void *workspace,
-                        cudaStream_t s);
+                        cudaStream_t s, bool sequential_stats = false);
 
 // Batched problems (rows [off[p], off[p+1]), seeds[p]); tp[p] = first row tile
 // of problem p, tiles of init_tile_rows() rows never straddle problems.
@@ -187,6 +216,10 @@ void launch_sgd_replay(const SgdArgs &args, int epoch, size_t nu, int64_t edge_b
                        cudaStream_t s);
 
 // ---- K8 NCE loss (the objective of src/ncvis.cpp:275-352) --------------------
+// Threads per block of the loss kernels; the workspace holds two FP64
+// partials per block plus two: nce_workspace_bytes(E) =
+// 16 * ((E + kNceThreads - 1) / kNceThreads + 1).
+constexpr int kNceThreads = 256;
 size_t nce_workspace_bytes(int64_t E);
 // mode 0: *out = loss (FP64 sum); mode 1: dY += (*scale) dL/dY (atomic FP32),
 // *out = (*scale) dL/dQ (FP64).

@@ -34,13 +34,17 @@ def _i32(t):
     return t.to(torch.int32).contiguous()
 
 
-def knn(X, k: int, distance: int = 0, precision: int = _lib.KNN_FP32, rerank_factor: int = 0):
+def knn(X, k: int, distance: int = 0, precision: int = _lib.KNN_FP32, rerank_factor: int = 0,
+        order: bool = True):
     """Exact kNN table (reference row contract, src/ncvis.cpp:128-153):
     returns (inds int32 [N, k], dists float32 [N, k]), rows in descending
-    distance order, the nearest of the k+1 dropped."""
+    distance order, the nearest of the k+1 dropped.  order=False keeps the
+    BF16 search in the caller's row order (no k-means cell ordering)."""
     torch = _torch()
     X = _f32(X)
     N, D = X.shape
+    if not order:
+        precision |= _lib.KNN_CALLER_ORDER
     inds = torch.empty((N, k), dtype=torch.int32, device=X.device)
     dists = torch.empty((N, k), dtype=torch.float32, device=X.device)
     _lib.check(_lib.lib().ncvis_knn_device(X.data_ptr(), N, D, distance, k, precision,
@@ -85,16 +89,19 @@ def symmetrize(inds, dists):
     return row_ptr, cols[:n], vals[:n], src[:n]
 
 
-def init_embedding(row_ptr, cols, d: int, seed: int, n_init_epochs: int, alpha: float):
+def init_embedding(row_ptr, cols, d: int, seed: int, n_init_epochs: int, alpha: float,
+                   sequential_stats: bool = False):
     """Y [N, d]: one-thread pcg64(seed) uniforms, then n_init_epochs of
-    neighbour averaging and standardisation (src/ncvis.cpp:184-273)."""
+    neighbour averaging and standardisation (src/ncvis.cpp:184-273);
+    sequential_stats: the statistics as the reference's one thread sums them."""
     torch = _torch()
     N = row_ptr.shape[0] - 1
     row_ptr = row_ptr.to(torch.int64).contiguous()
     cols = _i32(cols)
     Y = torch.empty((N, d), dtype=torch.float32, device=row_ptr.device)
     _lib.check(_lib.lib().ncvis_init_embedding_device(N, d, row_ptr.data_ptr(), cols.data_ptr(),
-                                                      seed, n_init_epochs, alpha, Y.data_ptr(),
+                                                      seed, n_init_epochs, alpha,
+                                                      int(bool(sequential_stats)), Y.data_ptr(),
                                                       _stream()))
     return Y
 

@@ -218,9 +218,24 @@ size_t orc_symmetrize(size_t N, size_t k, const int64_t *inds, const float *dist
 // src/ncvis.cpp:184-273.  Edges are (src[e], dst[e]) in build_edges order
 // (src/ncvis.cpp:155-173: the CSR rows flattened).  n_threads > 1 follows the
 // reference's parallel form (per-thread pcg64(seed + thread), static split);
-// n_threads == 1 is the deterministic form the GPU reproduces.
+// n_threads == 1 is the deterministic form the GPU reproduces.  stats64 != 0
+// (one thread only) is the checker of the engine's default statistics: the
+// same sums accumulated in double and rounded once (mean = (float)sum / N,
+// sigma = sqrtf((float)sum / N)), where the reference sums in float.
+void orc_init_embedding_stats(size_t N, size_t d, size_t E, const int64_t *src,
+                              const int64_t *dst, uint64_t seed, int n_init_epochs, float alpha,
+                              int n_threads, int stats64, float *Y);
+
 void orc_init_embedding(size_t N, size_t d, size_t E, const int64_t *src, const int64_t *dst,
                         uint64_t seed, int n_init_epochs, float alpha, int n_threads, float *Y) {
+    orc_init_embedding_stats(N, d, E, src, dst, seed, n_init_epochs, alpha, n_threads, 0, Y);
+}
+
+void orc_init_embedding_stats(size_t N, size_t d, size_t E, const int64_t *src,
+                              const int64_t *dst, uint64_t seed, int n_init_epochs, float alpha,
+                              int n_threads, int stats64, float *Y) {
+    if (stats64) n_threads = 1;
+    std::vector<double> acc(d);
     std::vector<float> other(N * d);
     float *bufs[2] = {Y, other.data()};
     std::vector<float> mean(d), sigma(d);
@@ -242,26 +257,44 @@ void orc_init_embedding(size_t N, size_t d, size_t E, const int64_t *src, const 
             }
 #pragma omp single
             for (size_t q = 0; q < d; ++q) mean[q] = sigma[q] = 0;
-#pragma omp for schedule(static)
-            for (long long i = 0; i < (long long)N; ++i)
-                for (size_t q = 0; q < d; ++q) {
-#pragma omp atomic
-                    mean[q] += dst_y[i * d + q];
-                }
+            if (stats64) {
 #pragma omp single
-            for (size_t q = 0; q < d; ++q) mean[q] /= N;
-#pragma omp for schedule(static)
-            for (long long i = 0; i < (long long)N; ++i)
-                for (size_t q = 0; q < d; ++q) {
-                    float dev = dst_y[i * d + q] - mean[q];
-                    dev *= dev;
-#pragma omp atomic
-                    sigma[q] += dev;
+                {
+                    for (size_t q = 0; q < d; ++q) acc[q] = 0;
+                    for (size_t i = 0; i < N; ++i)
+                        for (size_t q = 0; q < d; ++q) acc[q] += (double)dst_y[i * d + q];
+                    for (size_t q = 0; q < d; ++q) mean[q] = (float)acc[q] / (float)N;
+                    for (size_t q = 0; q < d; ++q) acc[q] = 0;
+                    for (size_t i = 0; i < N; ++i)
+                        for (size_t q = 0; q < d; ++q) {
+                            float dev = dst_y[i * d + q] - mean[q];
+                            dev *= dev;
+                            acc[q] += (double)dev;
+                        }
+                    for (size_t q = 0; q < d; ++q) sigma[q] = sqrtf((float)acc[q] / (float)N);
                 }
+            } else {
+#pragma omp for schedule(static)
+                for (long long i = 0; i < (long long)N; ++i)
+                    for (size_t q = 0; q < d; ++q) {
+#pragma omp atomic
+                        mean[q] += dst_y[i * d + q];
+                    }
 #pragma omp single
-            for (size_t q = 0; q < d; ++q) {
-                sigma[q] /= N;
-                sigma[q] = sqrtf(sigma[q]);
+                for (size_t q = 0; q < d; ++q) mean[q] /= N;
+#pragma omp for schedule(static)
+                for (long long i = 0; i < (long long)N; ++i)
+                    for (size_t q = 0; q < d; ++q) {
+                        float dev = dst_y[i * d + q] - mean[q];
+                        dev *= dev;
+#pragma omp atomic
+                        sigma[q] += dev;
+                    }
+#pragma omp single
+                for (size_t q = 0; q < d; ++q) {
+                    sigma[q] /= N;
+                    sigma[q] = sqrtf(sigma[q]);
+                }
             }
 #pragma omp for schedule(static)
             for (long long i = 0; i < (long long)N; ++i)

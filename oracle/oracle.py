@@ -55,6 +55,8 @@ def lib():
         L.orc_symmetrize.restype = _sz
         L.orc_init_embedding.argtypes = [_sz, _sz, _sz, _i64p, _i64p, C.c_uint64, C.c_int,
                                          C.c_float, C.c_int, _f32p]
+        L.orc_init_embedding_stats.argtypes = [_sz, _sz, _sz, _i64p, _i64p, C.c_uint64, C.c_int,
+                                               C.c_float, C.c_int, C.c_int, _f32p]
         L.orc_negative_stream.argtypes = [_sz, _sz, _i64p, C.c_uint64, C.c_int, _u64p, _i32p]
         L.orc_negative_stream.restype = _sz
         L.orc_optimize.argtypes = [_sz, _sz, _sz, _i64p, _i64p, _f32p, C.POINTER(C.c_float),
@@ -158,12 +160,15 @@ def edges_from_csr(row_ptr: np.ndarray) -> np.ndarray:
 
 
 def init_embedding(N: int, d: int, src, dst, seed: int, n_init_epochs: int, alpha: float,
-                   n_threads: int = 1) -> np.ndarray:
+                   n_threads: int = 1, stats64: bool = False) -> np.ndarray:
+    """init_embedding as the reference computes it (src/ncvis.cpp:184-273);
+    stats64: one thread with the per-dimension sums in double, rounded once
+    (the checker of the engine's default statistics)."""
     src = np.ascontiguousarray(src, np.int64)
     dst = np.ascontiguousarray(dst, np.int64)
     Y = np.empty((N, d), np.float32)
-    lib().orc_init_embedding(N, d, src.shape[0], src, dst, seed, n_init_epochs, alpha,
-                             n_threads, Y)
+    lib().orc_init_embedding_stats(N, d, src.shape[0], src, dst, seed, n_init_epochs, alpha,
+                                   n_threads, int(bool(stats64)), Y)
     return Y
 
 
