@@ -48,3 +48,25 @@ def test_large_graph(cuda, oracle):
     ref = oracle.init_embedding(20000, 2, src, cols, 1234, 20, np.float32(1 / 15), 1)
     Y = _gpu_init(cuda, rp, cols, 2, 1234, 20, np.float32(1 / 15))
     np.testing.assert_allclose(Y, ref, rtol=0, atol=1e-5 * max(1.0, np.abs(ref).max()))
+
+
+def test_sequential_statistics(cuda, oracle):
+    """The statistics summed as the reference's one thread sums them (FP32,
+    rows in order) track the oracle's init at 1e-6 (and the default FP64
+    statistics the oracle's double sums)."""
+    X, _ = gmm(30000, 16, 10, 5.0, seed=2)
+    inds, dists = oracle.knn(oracle.preprocess(X, 0), 0, 15)
+    rp, cols, _ = oracle.symmetrize(inds, dists)
+    src = oracle.edges_from_csr(rp)
+    alpha = np.float32(1 / 15)
+    from ncvis_gb300 import stages
+    t_rp = cuda.tensor(rp.astype(np.int64), device="cuda")
+    t_cols = cuda.tensor(cols.astype(np.int32), device="cuda")
+    for d in (1, 2, 5):
+        ref = oracle.init_embedding(30000, d, src, cols, 7, 20, alpha, 1)
+        ref64 = oracle.init_embedding(30000, d, src, cols, 7, 20, alpha, 1, stats64=True)
+        Ys = stages.init_embedding(t_rp, t_cols, d, 7, 20, alpha, sequential_stats=True)
+        Yd = stages.init_embedding(t_rp, t_cols, d, 7, 20, alpha)
+        scale = max(1.0, np.abs(ref).max())
+        assert np.abs(Ys.cpu().numpy() - ref).max() <= 1e-6 * scale
+        assert np.abs(Yd.cpu().numpy() - ref64).max() <= 1e-6 * scale
