@@ -171,9 +171,13 @@ class NCVis:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h:
+        if not h:
+            return
+        self._h = None
+        try:
             _lib.lib().ncvis_destroy(h)
-            self._h = None
+        except (TypeError, AttributeError):
+            pass  # interpreter shutdown: the module's globals are already gone
 
     def _set_stream(self, stream_ptr):
         self._options.stream = stream_ptr

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
@@ -76,6 +77,29 @@ struct EventPair {
         NCVIS_CUDA(cudaEventElapsedTime(&t, a, b));
         return t;
     }
+};
+
+// NVTX ranges over the host-side enqueue of each pipeline stage, named
+// "ncvis.<stage>" (the reference's DEBUG stage timers, src/ncvis.cpp:370-437,
+// name the same stages).  A profiler filters kernels by them, e.g.
+// `ncu --nvtx --nvtx-include "ncvis.optimize/"`.  NVTX is header-only: without
+// a tool attached every call returns at once.  next() closes the open range
+// and opens the next one; the destructor closes the last (on error paths too).
+struct StageRanges {
+    bool open = false;
+    StageRanges() = default;
+    StageRanges(const StageRanges &) = delete;
+    StageRanges &operator=(const StageRanges &) = delete;
+    void next(const char *name) {
+        if (open) nvtxRangePop();
+        nvtxRangePushA(name);
+        open = true;
+    }
+    void close() {
+        if (open) nvtxRangePop();
+        open = false;
+    }
+    ~StageRanges() { close(); }
 };
 
 inline void require(bool ok, const std::string &msg, int code = kInvalidArgument) {

@@ -427,10 +427,13 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     float *dQ = (float *)(base + o_Q);
 
     Events ev;
+    StageRanges nv;
+    nv.next("ncvis.h2d");
     NCVIS_CUDA(cudaEventRecord(ev.ev[0], s));
     if (host && !read_host)
         NCVIS_CUDA(cudaMemcpyAsync((void *)dX, X, sizeof(float) * N * D, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
+    nv.next("ncvis.preprocess");
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
     launch_preprocess(dX, (int64_t)N, (int)D, dist, Xp, sqn, Xb, bf16 ? tp.ldb : 0, flag, s, Xc);
     NCVIS_CUDA(cudaEventRecord(ev.ev[2], s));
@@ -440,6 +443,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
+    nv.next("ncvis.knn");
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
     if (ivf)
         run_knn_ivf(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist,
@@ -454,8 +458,10 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
     else
         launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
+    nv.next("ncvis.rerank");
     launch_rerank(Xp, (int64_t)N, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
+    nv.next("ncvis.symmetrize");
     if (bf16) {
         int timeout = 0;
         NCVIS_CUDA(cudaMemcpyAsync(&timeout, flag + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -467,10 +473,12 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
                                      src, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[5], s));
 
+    nv.next("ncvis.init");
     const float init_alpha = (float)(1. / k);
     run_init_embedding((int64_t)N, d, row_ptr, cols, (uint64_t)p.random_seed, p.n_init_epochs,
                        init_alpha, dY, base + o_init, s, o.init_sequential_stats != 0);
     NCVIS_CUDA(cudaEventRecord(ev.ev[6], s));
+    nv.next("ncvis.optimize");
 
     NCVIS_CUDA(cudaMemsetAsync(dQ, 0, sizeof(float), s));
     SgdArgs g;
@@ -513,9 +521,11 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
             run_sgd_hogwild(g, 0, p.n_epochs, noise.data(), chains, base + o_sgd, s);
     }
     NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
+    nv.next("ncvis.d2h");
     if (host)
         NCVIS_CUDA(cudaMemcpyAsync(Y, dY, sizeof(float) * N * d, cudaMemcpyDeviceToHost, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[8], s));
+    nv.close();
     NCVIS_CUDA(cudaEventSynchronize(ev.ev[8]));
 
     times.h2d_ms = ev.ms(0, 1);
@@ -652,12 +662,15 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     float *Ytune = (float *)(base + o_Yt), *Qtune = (float *)(base + o_Qt);
 
     Events ev;
+    StageRanges nv;
+    nv.next("ncvis.batched.h2d");
     NCVIS_CUDA(cudaEventRecord(ev.ev[0], s));
     NCVIS_CUDA(cudaMemcpyAsync(d_off, h_off.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaMemcpyAsync(d_tq, h_tq.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaMemcpyAsync(d_ti, h_ti.data(), sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaMemcpyAsync(d_seed, h_seed.data(), sizeof(uint64_t) * B, cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaEventRecord(ev.ev[1], s));
+    nv.next("ncvis.batched.preprocess");
     NCVIS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, s));
     __nv_bfloat16 *Xb = bf16 ? (__nv_bfloat16 *)(base + o_Xb) : nullptr;
     __nv_bfloat16 *Xc = fold ? (__nv_bfloat16 *)(base + o_Xc) : nullptr;
@@ -669,6 +682,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
+    nv.next("ncvis.batched.knn");
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
     if (bf16) {
         // Problems at 256-aligned rows of a padded copy; one tensor-core launch
@@ -711,8 +725,10 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         launch_knn_select_f32(Xp, sqn, total, (int)D, dist, kp, cand_i, cand_d, s, seg);
     }
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
+    nv.next("ncvis.batched.rerank");
     launch_rerank(Xp, total, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
+    nv.next("ncvis.batched.symmetrize");
     const int64_t E = run_symmetrize(total, k, knn_i, knn_d, base + o_sym, row_ptr, cols, vals, src, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[5], s));
 
@@ -736,10 +752,12 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         return cp[B];
     };
 
+    nv.next("ncvis.batched.init");
     const float init_alpha = (float)(1. / k);
     run_init_embedding_batched(total, d, d_off, d_ti, (int)B, h_ti[B], d_seed, row_ptr, cols,
                                p.n_init_epochs, init_alpha, dY, base + o_init, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[6], s));
+    nv.next("ncvis.batched.optimize");
 
     SgdBatch g{};
     g.d = d;
@@ -760,9 +778,12 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     // block of chains within one problem.
     const bool staged = d <= 4 && o.sgd_mode == NCVIS_SGD_HOGWILD;
     int64_t n_blocks = 0;
-    auto set_layout = [&](int edges_per_chain) {
-        g.n_chains = chain_layout(edges_per_chain, h_cp);
-        const int64_t T = sgd_window_batched_threads();
+    int block_chains = 128;
+    // A shape: edges per chain (high 16 bits) and, staged, chains per block.
+    auto set_layout = [&](int shape) {
+        g.n_chains = chain_layout(shape >> 16, h_cp);
+        block_chains = shape & 0xffff;
+        const int64_t T = block_chains;
         h_bp.assign(B + 1, 0);
         for (size_t q = 0; q < B; ++q) h_bp[q + 1] = h_bp[q] + (h_cp[q + 1] - h_cp[q] + T - 1) / T;
         n_blocks = h_bp[B];
@@ -773,17 +794,24 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
     };
     auto run_epochs = [&](const SgdBatch &t, const size_t *plan, cudaStream_t st) {
         if (staged)
-            run_sgd_window_batched(t, d_bp, n_blocks, plan, st);
+            run_sgd_window_batched(t, d_bp, n_blocks, block_chains, plan, st);
         else
             run_sgd_hogwild_batched(t, plan, st);
     };
     if (p.n_epochs > 0 && E > 0) {
-        // Autotune edges per chain on a scratch copy of the embedding (one epoch each).
-        const std::string key = std::string(staged ? "sgd_batched_staged" : "sgd_batched") +
+        // Autotune the shape on a scratch copy of the embedding (one epoch
+        // each): edges per chain (16..128) and, with staged noise, chains per
+        // block (64, 128, 256: more chains share a window's copy-in and
+        // write-back, fewer leave more blocks for small problems).
+        const std::string key = std::string(staged ? "sgd_batched_staged_shape" : "sgd_batched") +
                                 " d=" + std::to_string(d) + " B=" + std::to_string(B) +
                                 " E~2^" + std::to_string((int)std::log2((double)std::max<int64_t>(E, 1)));
-        const int chosen = tuner.pick(key, {16, 32, 64, 128}, [&](int epc) {
-            set_layout(epc);
+        std::vector<int> shapes;
+        for (int epc : {16, 32, 64, 128})
+            for (int t : {64, 128, 256})
+                if (staged || t == 128) shapes.push_back(epc << 16 | t);
+        const int chosen = tuner.pick(key, shapes, [&](int shape) {
+            set_layout(shape);
             NCVIS_CUDA(cudaMemcpyAsync(Ytune, dY, sizeof(float) * total * d, cudaMemcpyDeviceToDevice, s));
             NCVIS_CUDA(cudaMemsetAsync(Qtune, 0, sizeof(float) * B, s));
             SgdBatch t = g;
@@ -828,6 +856,7 @@ void ncvis_engine::fit_batched(const float *dX, size_t D, const int64_t *offsets
         NCVIS_CUDA(cudaEventRecord(ev.ev[7], s));
     }
     NCVIS_CUDA(cudaEventRecord(ev.ev[8], s));
+    nv.close();
     NCVIS_CUDA(cudaEventSynchronize(ev.ev[8]));
     times.h2d_ms = ev.ms(0, 1);
     times.preprocess_ms = ev.ms(1, 2);

@@ -500,6 +500,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tmem_ld(tmem + ((uint32_t)(quad * 32) << 16) +
                                 (uint32_t)(acc * 256 + h * 128 + chunk * kC),
                             v);
+                    if (chunk == kCandTile / kC - 1) {
+                        // The tile's last columns are in registers: the
+                        // accumulator goes back to the MMA warp before their
+                        // scan, so the next MMAs into it start meanwhile.
+                        tmem_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&s.acc_empty[acc][h]);
+                    }
                     const int64_t cb = c0 + chunk * kC;
                     // Scores, lower is better: |c|^2 - 2<q,c> (squared L2) or
                     // -<q,c> (kept as +<q,c>, compared against -worst).
@@ -571,9 +579,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                         }
                     }
                 }
-                tmem_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&s.acc_empty[acc][h]);
                 acc ^= 1;
                 if (acc == 0) acc_phase ^= 1;
                 // Queues past half full are flushed here, after the accumulator

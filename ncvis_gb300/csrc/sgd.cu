@@ -17,7 +17,8 @@
 // read through L2 (ld.cg) so that chains on other SMs see each other's
 // updates as the reference's threads do; y_o -= dx is an L2 reduction
 // (red.add), y_i is kept in registers over a run of equal sources and
-// stored when the source changes.
+// written back when the source changes: stored if no one else changed the
+// row meanwhile, else as the chain's own change added to it (put_row).
 //
 // Replay mode (sgd_replay): one thread executes the one-thread reference
 // sample by sample, with the reference build's arithmetic grouping (noise
@@ -87,6 +88,31 @@ __device__ __forceinline__ void sub_row(float *Y, int64_t i, const Vec<D> &dx) {
 #pragma unroll
         for (int c = 0; c < D; ++c)
             asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p + c), "f"(-dx.v[c]) : "memory");
+    }
+}
+
+// Writes back a source row the chain held in registers (yi; it read yi0 when
+// it took the row): a plain store when Y still holds yi0, else only the
+// chain's change yi - yi0 is added, as an L2 reduction, so that the updates
+// other chains (or the block's window write-back) made to the row while it
+// was held are kept.  The reference's threads write every sample to Y at
+// once (src/ncvis.cpp:335-338), so theirs are lost only to true races; a
+// plain store of the held row would drop every update others made to it
+// during a run of its edges.  One chain with no window change to the row
+// stores yi bit for bit.
+template <int D>
+__device__ __forceinline__ void put_row(float *Y, int64_t i, const Vec<D> &yi, const Vec<D> &yi0) {
+    const Vec<D> now = load_row<D>(Y, i);
+    bool same = true;
+#pragma unroll
+    for (int c = 0; c < D; ++c) same &= __float_as_uint(now.v[c]) == __float_as_uint(yi0.v[c]);
+    if (same) {
+        store_row<D>(Y, i, yi);
+    } else {
+        Vec<D> back;  // yi0 - yi: sub_row adds yi - yi0
+#pragma unroll
+        for (int c = 0; c < D; ++c) back.v[c] = yi0.v[c] - yi.v[c];
+        sub_row<D>(Y, i, back);
     }
 }
 
@@ -211,8 +237,7 @@ __device__ __forceinline__ void run_edge(float *Y, Vec<D> &yi, uint32_t i, uint3
 // A chain's edges [e0, e1) (e0 a multiple of 4): edge indices come in aligned
 // groups of four, the next group loaded while the current one runs; y_i stays
 // in registers while consecutive edges share their source row and is written
-// back when the row changes (other chains' updates of that row in between are
-// lost, as lock-free updates may be).
+// back (put_row) when the row changes.
 template <int D>
 __device__ __forceinline__ void run_chain(float *Y, const int32_t *__restrict__ src,
                                           const int32_t *__restrict__ dst, int64_t e0, int64_t e1,
@@ -238,6 +263,7 @@ __device__ __forceinline__ void run_chain(float *Y, const int32_t *__restrict__ 
     load4(e0, s4, d4);
     uint32_t cur = (uint32_t)s4.x;
     Vec<D> yi = load_row<D>(Y, cur);
+    Vec<D> yi0 = yi;
     for (int64_t e = e0; e < e1; e += 4) {
         int4 ns4 = s4, nd4 = d4;
         if (e + 4 < e1) load4(e + 4, ns4, nd4);
@@ -248,16 +274,17 @@ __device__ __forceinline__ void run_chain(float *Y, const int32_t *__restrict__ 
             if (e + q >= e1) break;
             const uint32_t i = (uint32_t)sv[q];
             if (i != cur) {
-                store_row<D>(Y, cur, yi);
+                put_row<D>(Y, cur, yi, yi0);
                 cur = i;
                 yi = load_row<D>(Y, cur);
+                yi0 = yi;
             }
             run_edge<D>(Y, yi, i, (uint32_t)dv[q], e + q, N, lo, k, Qc, key0, key1, tag);
         }
         s4 = ns4;
         d4 = nd4;
     }
-    store_row<D>(Y, cur, yi);
+    put_row<D>(Y, cur, yi, yi0);
 }
 
 template <int D>
@@ -356,9 +383,10 @@ __global__ void __launch_bounds__(kThreads) sgd_epoch_batched(
         const int64_t a = min(e1, (e0 + 3) & ~(int64_t)3);
         for (int64_t e = e0; e < a; ++e) {
             Vec<D> yi = load_row<D>(Y, (uint32_t)src[e]);
+            const Vec<D> yi0 = yi;
             run_edge<D>(Y, yi, (uint32_t)src[e], (uint32_t)dst[e], e, Np, lo, k, Qc, key0, key1,
                         (uint32_t)epoch);
-            store_row<D>(Y, (uint32_t)src[e], yi);
+            put_row<D>(Y, (uint32_t)src[e], yi, yi0);
         }
         run_chain<D>(Y, src, dst, a, e1, Np, lo, k, Qc, key0, key1, (uint32_t)epoch);
     }
@@ -558,7 +586,8 @@ __device__ __forceinline__ void gather_group(const float *Y, const int32_t (&sv)
 }
 
 // Edges [a, b) of a chain (a a multiple of 4) against the round's window; the
-// chain's current source row (ci, yi, valid when `have`) carries over rounds.
+// chain's current source row (ci, yi, read as yi0; valid when `have`) carries
+// over rounds and is written back by put_row.
 // The positive rows of a group of four edges are gathered together before the
 // group runs (one memory round trip per group instead of one per edge); a
 // gathered row that this chain wrote in between (an earlier positive row or
@@ -570,7 +599,7 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
                                              const EpochConst &k, float &Qc, uint32_t key0,
                                              uint32_t key1, uint32_t tag, float *win,
                                              const WindowSpec &ws, bool &have, uint32_t &ci,
-                                             Vec<D> &yi) {
+                                             Vec<D> &yi, Vec<D> &yi0) {
     for (int64_t e = a; e < b; e += 4) {
         int32_t sv[4], dv[4];
         load_group(src, dst, e, b, sv, dv);
@@ -582,9 +611,10 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
             if (e + q >= b) break;
             const uint32_t i = (uint32_t)sv[q], j = (uint32_t)dv[q];
             if (!have || i != ci) {
-                if (have) store_row<D>(Y, ci, yi);
+                if (have) put_row<D>(Y, ci, yi, yi0);
                 ci = i;
                 yi = load_row<D>(Y, ci);
+                yi0 = yi;
                 have = true;
             }
             if (j != i) {
@@ -662,9 +692,9 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
     float Qc = *Q_in;
     bool have = false;
     uint32_t ci = 0;
-    Vec<D> yi;
+    Vec<D> yi, yi0;
 #pragma unroll
-    for (int c = 0; c < D; ++c) yi.v[c] = 0.f;
+    for (int c = 0; c < D; ++c) yi.v[c] = yi0.v[c] = 0.f;
     for (int r = 0; r < rounds; ++r) {
         for (uint32_t t = threadIdx.x; t < nseg; t += kWinThreads)
             seg[t] = segment_start(key0, key1, blockIdx.x, (uint32_t)r, (uint32_t)epoch, t, N);
@@ -679,7 +709,7 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
         const int64_t b = min(e1, a + round_edges);
         const WindowSpec ws{seg, W, N, 0u, false};
         window_edges<D, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                               have, ci, yi);
+                               have, ci, yi, yi0);
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < W; u += kWinThreads) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
@@ -694,7 +724,7 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
         }
         __syncthreads();
     }
-    if (have) store_row<D>(Y, ci, yi);
+    if (have) put_row<D>(Y, ci, yi, yi0);
     __shared__ double red[kWinThreads / 32];
     double v = chain < n_chains ? (double)Qc : 0.0;
 #pragma unroll
@@ -712,12 +742,12 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
 // problem (problem p owns blocks [bp[p], bp[p+1]) and chains [cp[p], cp[p+1]),
 // the last block of a problem partly idle); the window is the problem's rows
 // when they fit (exact uniform picks over them) or 256-row segments at uniform
-// starts within the problem otherwise.
-constexpr int kBatThreads = 128;
+// starts within the problem otherwise.  Blocks of T chains (T in 64, 128,
+// 256: the engine's autotuner picks T with the edges per chain).
 constexpr uint32_t kBatWindow = 1024;  // rows; two copies of d <= 4 floats fit 32 KB
 
-template <int D>
-__global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
+template <int D, int T>
+__global__ void __launch_bounds__(T) sgd_epoch_window_batched(
     float *__restrict__ Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
     const int64_t *__restrict__ off, const int64_t *__restrict__ eoff,
     const int64_t *__restrict__ cp, const int64_t *__restrict__ bp, int B,
@@ -727,7 +757,7 @@ __global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
     __shared__ __align__(16) float loaded[kBatWindow * D];
     __shared__ uint32_t seg[kBatWindow / kSegRows];
     const int p = segment_of(bp, B, (int64_t)blockIdx.x);
-    const int64_t lc = ((int64_t)blockIdx.x - bp[p]) * kBatThreads + threadIdx.x;
+    const int64_t lc = ((int64_t)blockIdx.x - bp[p]) * T + threadIdx.x;
     const int64_t nc = cp[p + 1] - cp[p];
     const int64_t Ep = eoff[p + 1] - eoff[p];
     const int64_t chunk = ((Ep + nc - 1) / nc + 3) & ~(int64_t)3;
@@ -743,15 +773,15 @@ __global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
     float Qc = Qs[p];
     bool have = false;
     uint32_t ci = 0;
-    Vec<D> yi;
+    Vec<D> yi, yi0;
 #pragma unroll
-    for (int c = 0; c < D; ++c) yi.v[c] = 0.f;
+    for (int c = 0; c < D; ++c) yi.v[c] = yi0.v[c] = 0.f;
     for (int r = 0; r < rounds; ++r) {
         if (!whole)
-            for (uint32_t t = threadIdx.x; t < W / kSegRows; t += kBatThreads)
+            for (uint32_t t = threadIdx.x; t < W / kSegRows; t += T)
                 seg[t] = segment_start(key0, key1, blockIdx.x, (uint32_t)r, (uint32_t)epoch, t, Np);
         __syncthreads();
-        for (uint32_t u = threadIdx.x; u < W; u += kBatThreads) {
+        for (uint32_t u = threadIdx.x; u < W; u += T) {
             const Vec<D> v = load_row<D>(Y, spec_row(ws, u));
             store_win<D>(win, u, v);
             store_win<D>(loaded, u, v);
@@ -761,12 +791,12 @@ __global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
         const int64_t b = min(e1, a + round_edges);
         if (whole)
             window_edges<D, true>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                                  have, ci, yi);
+                                  have, ci, yi, yi0);
         else
             window_edges<D, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                                   have, ci, yi);
+                                   have, ci, yi, yi0);
         __syncthreads();
-        for (uint32_t u = threadIdx.x; u < W; u += kBatThreads) {
+        for (uint32_t u = threadIdx.x; u < W; u += T) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
             Vec<D> minus;
             bool moved = false;
@@ -779,7 +809,7 @@ __global__ void __launch_bounds__(kBatThreads) sgd_epoch_window_batched(
         }
         __syncthreads();
     }
-    if (have) store_row<D>(Y, ci, yi);
+    if (have) put_row<D>(Y, ci, yi, yi0);
     if (active) chain_q[cp[p] + lc] = Qc;
 }
 
@@ -968,6 +998,13 @@ uint32_t sgd_window_rows(int d) {
     return w;
 }
 
+// Dynamic shared memory of sgd_epoch_window: the window and its loaded copy,
+// the segment starts.
+size_t window_smem_bytes(int d) {
+    const uint32_t W = sgd_window_rows(d);
+    return (size_t)W * d * 8 + (W / kSegRows) * 4;
+}
+
 bool sgd_window_applies(int64_t N, int d) {
     return d >= 1 && d <= 4 && N >= 16 * (int64_t)sgd_window_rows(d);
 }
@@ -986,8 +1023,7 @@ void launch_window_epoch(unsigned blocks, size_t smem, cudaStream_t s, const Sgd
 }
 
 int64_t window_resident_chains(int d) {
-    const uint32_t W = sgd_window_rows(d);
-    const size_t smem = (size_t)W * d * 8 + (W / kSegRows) * 4;
+    const size_t smem = window_smem_bytes(d);
     int blocks = 0;
     cudaError_t err;
     auto occ = [&](auto kernel) {
@@ -1023,7 +1059,7 @@ void run_sgd_window(const SgdArgs &g, int epoch_begin, int epoch_end, const size
     if (round_edges <= 0) round_edges = 16;
     round_edges = (round_edges + 3) & ~3;
     const uint32_t W = sgd_window_rows(g.d);
-    const size_t smem = (size_t)W * g.d * 8 + (W / kSegRows) * 4;
+    const size_t smem = window_smem_bytes(g.d);
     const unsigned blocks = ceil_div(chains, kWinThreads);
     const int64_t total_chains = chains;
     const int64_t chunk = ((g.E + total_chains - 1) / total_chains + 3) & ~(int64_t)3;
@@ -1053,11 +1089,34 @@ void run_sgd_window(const SgdArgs &g, int epoch_begin, int epoch_end, const size
     }
 }
 
-int sgd_window_batched_threads() { return kBatThreads; }
+bool sgd_window_batched_threads_ok(int threads) {
+    return threads == 64 || threads == 128 || threads == 256;
+}
 
-void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks,
+template <int D, int T>
+void launch_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks,
+                           const EpochConst &k, int ep, uint32_t key0, uint32_t key1,
+                           int round_edges, cudaStream_t s) {
+    NCVIS_LAUNCH((sgd_epoch_window_batched<D, T>), (unsigned)n_blocks, T, 0, s, g.Y, g.src, g.dst,
+                 g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k, ep, key0, key1, round_edges);
+}
+
+template <int D>
+void launch_window_batched_t(const SgdBatch &g, const int64_t *bp, int64_t n_blocks, int threads,
+                             const EpochConst &k, int ep, uint32_t key0, uint32_t key1,
+                             int round_edges, cudaStream_t s) {
+    switch (threads) {
+        case 64: launch_window_batched<D, 64>(g, bp, n_blocks, k, ep, key0, key1, round_edges, s); break;
+        case 128: launch_window_batched<D, 128>(g, bp, n_blocks, k, ep, key0, key1, round_edges, s); break;
+        default: launch_window_batched<D, 256>(g, bp, n_blocks, k, ep, key0, key1, round_edges, s);
+    }
+}
+
+void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks, int threads,
                             const size_t *n_noise, cudaStream_t s) {
     require(g.d >= 1 && g.d <= 4, "batched optimize: d must be in [1, 4]");
+    require(sgd_window_batched_threads_ok(threads),
+            "batched optimize: chains per block must be 64, 128 or 256");
     uint32_t key0, key1;
     noise_key(g.seed, key0, key1);
     const int round_edges = 16;
@@ -1066,25 +1125,10 @@ void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_bloc
                     g.a, g.b, g.alpha, g.alpha_Q};
         EpochConst k = epoch_const(one, ep, (int)n_noise[ep]);
         switch (g.d) {
-            case 1:
-                NCVIS_LAUNCH(sgd_epoch_window_batched<1>, (unsigned)n_blocks, kBatThreads, 0, s,
-                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
-                             ep, key0, key1, round_edges);
-                break;
-            case 2:
-                NCVIS_LAUNCH(sgd_epoch_window_batched<2>, (unsigned)n_blocks, kBatThreads, 0, s,
-                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
-                             ep, key0, key1, round_edges);
-                break;
-            case 3:
-                NCVIS_LAUNCH(sgd_epoch_window_batched<3>, (unsigned)n_blocks, kBatThreads, 0, s,
-                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
-                             ep, key0, key1, round_edges);
-                break;
-            default:
-                NCVIS_LAUNCH(sgd_epoch_window_batched<4>, (unsigned)n_blocks, kBatThreads, 0, s,
-                             g.Y, g.src, g.dst, g.off, g.eoff, g.cp, bp, g.B, g.Qs, g.chain_q, k,
-                             ep, key0, key1, round_edges);
+            case 1: launch_window_batched_t<1>(g, bp, n_blocks, threads, k, ep, key0, key1, round_edges, s); break;
+            case 2: launch_window_batched_t<2>(g, bp, n_blocks, threads, k, ep, key0, key1, round_edges, s); break;
+            case 3: launch_window_batched_t<3>(g, bp, n_blocks, threads, k, ep, key0, key1, round_edges, s); break;
+            default: launch_window_batched_t<4>(g, bp, n_blocks, threads, k, ep, key0, key1, round_edges, s);
         }
         NCVIS_LAUNCH(reduce_q_batched, g.B, 256, 0, s, g.chain_q, g.cp, g.Qs);
     }

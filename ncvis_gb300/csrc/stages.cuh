@@ -204,10 +204,10 @@ struct SgdBatch {
 };
 void run_sgd_hogwild_batched(const SgdBatch &g, const size_t *n_noise, cudaStream_t s);
 // The same with the noise staged in shared memory (d <= 4): problem p's chains
-// [cp[p], cp[p+1]) run in blocks [bp[p], bp[p+1]) of sgd_window_batched_threads()
-// (device array bp of B + 1 entries, n_blocks = bp[B]).
-int sgd_window_batched_threads();
-void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks,
+// [cp[p], cp[p+1]) run in blocks [bp[p], bp[p+1]) of `threads` chains each
+// (64, 128 or 256; device array bp of B + 1 entries, n_blocks = bp[B]).
+bool sgd_window_batched_threads_ok(int threads);
+void run_sgd_window_batched(const SgdBatch &g, const int64_t *bp, int64_t n_blocks, int threads,
                             const size_t *n_noise, cudaStream_t s);
 int64_t sgd_batched_resident_chains(int d);
 // *err (device int) is set to 1 if an index outside [0, N) is met.

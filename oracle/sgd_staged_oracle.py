@@ -18,7 +18,9 @@ Philox block, masked to the power-of-two window size; a pick whose row is the
 edge source is redrawn); noise updates go to
 the window, and the window's change is added to Y at the end of the round.
 The source row is held aside (as the kernel holds it in registers) and
-written back when the source changes and after the last round.
+written back when the source changes and after the last round: stored when
+Y still holds the value the chain read, else the chain's change is added
+(a window write-back may have changed the row meanwhile).
 """
 from __future__ import annotations
 
@@ -88,6 +90,14 @@ def _weight(d2, positive, nu, step, a, b, alpha_Q, Q):
     return w * step, Q
 
 
+def _put(Y, ci, yi, yi0):
+    """The kernel's write-back of a held source row (put_row)."""
+    if np.array_equal(Y[ci], yi0):
+        Y[ci] = yi
+    else:
+        Y[ci] += yi - yi0
+
+
 def optimize_staged_one_chain(Y, Q, src, dst, seed, n_noise, a, b, alpha=1.0, alpha_Q=1.0,
                               epoch_begin=0, epoch_end=None, round_edges=8):
     """Y [N, d] and Q after epochs [epoch_begin, epoch_end) of the staged
@@ -111,7 +121,7 @@ def optimize_staged_one_chain(Y, Q, src, dst, seed, n_noise, a, b, alpha=1.0, al
         nu = plan[ep]
         frac = float(np.float32(ep) / np.float32(n_epochs))
         step = alpha * (1.0 - frac * frac)
-        have, ci, yi = False, 0, None
+        have, ci, yi, yi0 = False, 0, None, None
         for r in range(rounds):
             seg = _segments(k0, k1, 0, r, ep, W, N)
             rows = np.array([_row(seg, u, N) for u in range(W)], dtype=np.int64)
@@ -123,8 +133,9 @@ def optimize_staged_one_chain(Y, Q, src, dst, seed, n_noise, a, b, alpha=1.0, al
                 i, j = int(src[e]), int(dst[e])
                 if not have or i != ci:
                     if have:
-                        Y[ci] = yi
+                        _put(Y, ci, yi, yi0)
                     ci, yi, have = i, Y[i].copy(), True
+                    yi0 = yi.copy()
                 if j != i:
                     yj = Y[j].copy()
                     diff = yi - yj
@@ -148,5 +159,5 @@ def optimize_staged_one_chain(Y, Q, src, dst, seed, n_noise, a, b, alpha=1.0, al
                         win[u] = yo - dx
             np.add.at(Y, rows, win - loaded)
         if have:
-            Y[ci] = yi
+            _put(Y, ci, yi, yi0)
     return Y, Q
