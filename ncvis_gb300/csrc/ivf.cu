@@ -266,8 +266,10 @@ struct Cells {
 
 // Step 1: `iters` k-means moves of C centroids (initial centroids: rows drawn
 // with Philox from `seed`), each after an assignment by the tensor-core
-// selection kernel, and a final assignment: point i's cell is cand[i * 32].
+// selection kernel, and a final assignment: point i's cell is cand[i * kAssignR].
 // Centroids are unit length for cosine and correlation.
+constexpr int kAssignR = 8;  // candidates kept per point by the cell assignment
+
 void kmeans_cells(const float *Xp, const __nv_bfloat16 *Xb, int64_t N, int D,
                   const KnnTcPlan &tp, int dist, int C, int iters, uint64_t seed, int32_t *cand,
                   int *timeout_flag, cudaStream_t s, DeviceArena &arena, Cells &cells) {
@@ -285,8 +287,10 @@ void kmeans_cells(const float *Xp, const __nv_bfloat16 *Xb, int64_t N, int D,
     NCVIS_LAUNCH(ivf_init, warps_c, 256, 0, s, Xp, N, D, C, k0, k1, cent);
     NCVIS_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * C * D, s));
     NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
+    // The assignment needs each point's nearest centroid only: the selection
+    // keeps 8 (its shortest list), entry 0 of each row is the cell.
     KnnTcPlan ap = tp;
-    ap.R = 32;
+    ap.R = kAssignR;
     const TcWork awork = upload(all_pairs_work(N, C), nullptr, arena);
     const int normalise = (dist == kCosine || dist == kCorrelation) ? 1 : 0;
     // Per-block sums in shared memory where C * D floats fit in 110 KB (two
@@ -305,10 +309,10 @@ void kmeans_cells(const float *Xp, const __nv_bfloat16 *Xb, int64_t N, int D,
         if (pass == iters) break;
         if (shared_acc)
             NCVIS_LAUNCH(ivf_accumulate_shared, (unsigned)(2 * num_sms()), 512, acc_smem, s, Xp,
-                         N, D, cand, 32, C, sums, counts);
+                         N, D, cand, kAssignR, C, sums, counts);
         else
             NCVIS_LAUNCH(ivf_accumulate, (unsigned)ceil_div((size_t)N, 8), 256, 0, s, Xp, N, D,
-                         cand, 32, C, sums, counts);
+                         cand, kAssignR, C, sums, counts);
         NCVIS_LAUNCH(ivf_update, warps_c, 256, 0, s, cent, sums, counts, C, D, normalise);
     }
 }
@@ -327,7 +331,7 @@ void sort_by_cell(const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc, int64_t N, i
     cells.Xs = arena.alloc<__nv_bfloat16>((size_t)N * ldb);
     cells.Xcs = Xc ? arena.alloc<__nv_bfloat16>((size_t)N * ldb) : nullptr;
     NCVIS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * C, s));
-    NCVIS_LAUNCH(ivf_count, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, 32, N, C,
+    NCVIS_LAUNCH(ivf_count, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, kAssignR, N, C,
                  counts);
     cells.counts.assign(C, 0);
     NCVIS_CUDA(cudaMemcpyAsync(cells.counts.data(), counts, sizeof(int) * C,
@@ -340,7 +344,7 @@ void sort_by_cell(const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc, int64_t N, i
     NCVIS_CUDA(cudaMemcpyAsync(d_starts, cells.starts.data(), sizeof(int64_t) * (C + 1),
                                cudaMemcpyHostToDevice, s));
     NCVIS_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * C, s));
-    NCVIS_LAUNCH(ivf_scatter, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, 32, N, C,
+    NCVIS_LAUNCH(ivf_scatter, (unsigned)ceil_div((size_t)N, 256), 256, 0, s, cand, kAssignR, N, C,
                  d_starts, cursor, cells.perm);
     const size_t vec = (size_t)N * (ldb / 8);
     NCVIS_LAUNCH(ivf_gather_rows, (unsigned)ceil_div(vec, 256), 256, 0, s, Xb, cells.perm, N, ldb,

@@ -680,7 +680,9 @@ void launch_select(const CUtensorMap &map, const CUtensorMap &map_c, const float
                      work_begin, items, row_map, cand_i, timeout_flag,
                      plan.wait_cycles > 0 ? plan.wait_cycles : kWaitCycles, plan.stall ? 1 : 0);
     };
-    if (plan.R == 32)
+    if (plan.R == 8)
+        ip ? go(knn_select_tc<8, true>) : go(knn_select_tc<8, false>);
+    else if (plan.R == 32)
         ip ? go(knn_select_tc<32, true>) : go(knn_select_tc<32, false>);
     else
         ip ? go(knn_select_tc<64, true>) : go(knn_select_tc<64, false>);
@@ -690,7 +692,8 @@ void check_plan(const KnnTcPlan &plan) {
     const int ksteps = (plan.ldb + 15) / 16;
     const int katoms = (ksteps * 16 + 63) / 64;
     require(katoms <= kMaxAtoms, "knn: the tensor-core path supports D <= 128", kUnsupported);
-    require(plan.R == 32 || plan.R == 64, "knn: the tensor-core kernel keeps 32 or 64 candidates");
+    require(plan.R == 8 || plan.R == 32 || plan.R == 64,
+            "knn: the tensor-core kernel keeps 8, 32 or 64 candidates");
 }
 
 }  // namespace
