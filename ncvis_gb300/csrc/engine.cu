@@ -444,6 +444,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         require(bad == 0, "[ncvis] input contains non-finite values");
     }
     nv.next("ncvis.knn");
+    const int32_t *cell_order = nullptr;  // rows in k-means cell order (ordered sweep only)
     NCVIS_CUDA(cudaMemsetAsync(knn_i, 0xff, sizeof(int32_t) * nk, s));
     if (ivf)
         run_knn_ivf(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist,
@@ -451,7 +452,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
                     cand_i, flag + 2, s);
     else if (op.C > 0)
         run_knn_tc_ordered(Xp, Xb, Xc, (int64_t)N, (int)D, tp, dist, op, (uint64_t)p.random_seed,
-                           cand_i, flag + 2, s, base + o_ord, ord_bytes, ev.ev[9]);
+                           cand_i, flag + 2, s, base + o_ord, ord_bytes, ev.ev[9], &cell_order);
     else if (bf16)
         launch_knn_select_tc(Xb, sqn, (int64_t)N, tp, dist, cand_i, cand_d, flag + 2, s, nullptr,
                              Xc);
@@ -459,7 +460,7 @@ void ncvis_engine::fit(const float *X, size_t N, size_t D, float *Y, bool host) 
         launch_knn_select_f32(Xp, sqn, (int64_t)N, (int)D, dist, kp, cand_i, cand_d, s);
     NCVIS_CUDA(cudaEventRecord(ev.ev[3], s));
     nv.next("ncvis.rerank");
-    launch_rerank(Xp, (int64_t)N, (int)D, dist, cand_i, C, k, knn_i, knn_d, s);
+    launch_rerank(Xp, (int64_t)N, (int)D, dist, cand_i, C, k, knn_i, knn_d, s, cell_order);
     NCVIS_CUDA(cudaEventRecord(ev.ev[4], s));
     nv.next("ncvis.symmetrize");
     if (bf16) {
@@ -996,6 +997,7 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         NCVIS_CUDA(cudaStreamSynchronize(s));
         require(!bad, "knn: input contains non-finite values");
         NCVIS_CUDA(cudaMemsetAsync(d_inds, 0xff, sizeof(int32_t) * N * k, s));
+        const int32_t *cell_order = nullptr;
         if (ivf) {
             run_knn_ivf((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
                         plan_ivf((int64_t)N, lists, probe), 42, (int32_t *)(base + o_ci),
@@ -1003,7 +1005,7 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
         } else if (op.C > 0) {
             run_knn_tc_ordered((float *)(base + o_Xp), Xb, Xc, (int64_t)N, (int)D, tp, distance,
                                op, 42, (int32_t *)(base + o_ci), (int *)(base + o_flag) + 1, s,
-                               base + o_ord, ord_bytes);
+                               base + o_ord, ord_bytes, nullptr, &cell_order);
         } else if (bf16) {
             launch_knn_select_tc(Xb, (float *)(base + o_sqn), (int64_t)N, tp, distance,
                                  (int32_t *)(base + o_ci), (float *)(base + o_cd),
@@ -1020,7 +1022,7 @@ void knn_device(const float *dX, size_t N, size_t D, int distance, size_t k, int
                                   (float *)(base + o_cd), s);
         }
         launch_rerank((float *)(base + o_Xp), (int64_t)N, (int)D, distance,
-                      (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s);
+                      (int32_t *)(base + o_ci), C, (int)k, d_inds, d_dists, s, cell_order);
     }
 }
 

@@ -507,7 +507,8 @@ size_t knn_order_workspace_bytes(int64_t N, int D, const KnnTcPlan &tp, const Kn
 void run_knn_tc_ordered(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfloat16 *Xc,
                         int64_t N, int D, const KnnTcPlan &tp, int dist, const KnnOrderPlan &op,
                         uint64_t seed, int32_t *cand_i, int *timeout_flag, cudaStream_t s,
-                        void *workspace, size_t workspace_bytes, cudaEvent_t sweep_start) {
+                        void *workspace, size_t workspace_bytes, cudaEvent_t sweep_start,
+                        const int32_t **cell_order) {
     require(op.C > 0, "knn: ordered search without cells", kInternal);
     require(N < (int64_t(1) << 31), "knn: N must be below 2^31");
     require(num_sms() <= 1024, "knn: more SMs than the ordered search's work list allows",
@@ -549,6 +550,9 @@ void run_knn_tc_ordered(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfl
     launch_knn_select_tc_pair(cells.Xs, N, fold ? cells.Xcs : cells.Xs, N, nullptr, tp, true,
                               cand_i, timeout_flag, s, sweep);
     check_timeout(timeout_flag, s);
+    // The rows in cell order (sorted position -> row), for the caller's
+    // rerank; only from a caller's workspace, which outlives this call.
+    if (cell_order) *cell_order = workspace ? cells.perm : nullptr;
 }
 
 }  // namespace ncvis_gpu

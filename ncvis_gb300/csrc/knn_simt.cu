@@ -240,13 +240,17 @@ template <int T>  // ceil(D / 32) coordinates per lane, T <= 4; T == 0: any D
 __global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp, int64_t N, int D,
                                                    int dist, const int32_t *__restrict__ cand_i,
                                                    int C, int k, int32_t *__restrict__ inds,
-                                                   float *__restrict__ dists) {
+                                                   float *__restrict__ dists,
+                                                   const int32_t *__restrict__ order) {
     extern __shared__ __align__(16) char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
     float *sd = (float *)smem_raw + (size_t)warp * C * 2;
     int *si = (int *)(sd + C);
-    if (row >= N) return;
+    if (w >= N) return;
+    // Rows in `order` (a permutation of [0, N)) when given: neighbouring points
+    // then run together and share their candidates' rows in L2.
+    const int64_t row = order ? (int64_t)order[w] : w;
     const float *q = Xp + row * D;
     const bool l2 = (dist == kSquaredL2);
     float qv[T > 0 ? T : 1];
@@ -366,7 +370,7 @@ void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int 
 }
 
 void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,
-                   int k, int32_t *inds, float *dists, cudaStream_t s) {
+                   int k, int32_t *inds, float *dists, cudaStream_t s, const int32_t *order) {
     require(C <= 1024, "rerank: too many candidates per point");
     const int warps = 4;
     const size_t smem = (size_t)warps * C * 8;
@@ -375,7 +379,8 @@ void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *c
     // cached flag shared between host threads).
     auto go = [&](auto kernel) {
         NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        NCVIS_LAUNCH(kernel, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists);
+        NCVIS_LAUNCH(kernel, grid, warps * 32, smem, s, Xp, N, D, dist, cand_i, C, k, inds, dists,
+                     order);
     };
     switch ((D + 31) / 32) {
         case 1: go(rerank_rows<1>); break;

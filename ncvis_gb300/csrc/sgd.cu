@@ -119,28 +119,44 @@ __device__ __forceinline__ void put_row(float *Y, int64_t i, const Vec<D> &yi, c
 struct EpochConst {
     float step, nu_f, a, b, ab, alpha_Q, pow_b1_at_zero;
     int nu;
+    float b1, ab2;  // b - 1 and 2ab
 };
 
 // The update weight of one sample (w * step), Q copy updated in place.
+// With Ph = 1/denom, denom = 1 + a d2^b, nm = nu e^Q and t = 1 + nm denom:
+//   noise:    w = -1/t,      final weight -(2ab) d2^(b-1) / (t denom)
+//   positive: w = 1 - 1/t,   final weight (2ab) d2^(b-1) w / denom
+// (the reference's 1/(1 + Ph/nm) and -1/(1 + nm/Ph), src/ncvis.cpp:309-321),
+// so one reciprocal, r = 1/(t denom), serves both Q's update and the weight;
+// d2^b and d2^(b-1) come from one log2.
 __device__ __forceinline__ float nce_weight(float d2, bool positive, const EpochConst &k,
                                             float &Qc) {
+    // Every product is rounded on its own (no contraction the compiler may
+    // choose per call site), so each kernel that calls this computes the
+    // same bits for the same inputs.
     if (k.nu == 0) return k.step;
     float p, p1;
     if (d2 > 0.f) {
-        p = exp2f(k.b * __log2f(d2));
-        p1 = __fdividef(p, d2);
+        const float lg = __log2f(d2);
+        p = exp2f(__fmul_rn(k.b, lg));
+        p1 = exp2f(__fmul_rn(k.b1, lg));
     } else {
         p = 0.f;
         p1 = k.pow_b1_at_zero;
     }
     const float denom = fmaf(k.a, p, 1.f);
-    const float ph = __fdividef(1.f, denom);
-    const float nm = k.nu_f * __expf(Qc);
-    float w = positive ? __fdividef(1.f, __fdividef(ph, nm) + 1.f)
-                       : -__fdividef(1.f, fmaf(nm, denom, 1.f));
-    Qc = fmaf(-w, k.alpha_Q, Qc);
-    w = w * p1 * (2.f * k.ab * ph);
-    return w * k.step;
+    const float t = fmaf(__fmul_rn(k.nu_f, __expf(Qc)), denom, 1.f);
+    const float r = __fdividef(1.f, __fmul_rn(t, denom));
+    float w;
+    if (positive) {
+        w = fmaf(-r, denom, 1.f);  // 1 - 1/t
+        Qc = fmaf(-w, k.alpha_Q, Qc);
+        w = __fmul_rn(__fmul_rn(w, p1), __fmul_rn(k.ab2, __fmul_rn(r, t)));  // r t = 1/denom
+    } else {
+        Qc = fmaf(__fmul_rn(r, denom), k.alpha_Q, Qc);  // r denom = 1/t
+        w = -__fmul_rn(__fmul_rn(p1, k.ab2), r);
+    }
+    return __fmul_rn(w, k.step);
 }
 
 template <int D>
@@ -910,6 +926,8 @@ EpochConst epoch_const(const SgdArgs &g, int epoch, int nu) {
     k.ab = g.a * g.b;
     k.alpha_Q = g.alpha_Q;
     k.pow_b1_at_zero = std::pow(0.f, g.b - 1.f);
+    k.b1 = g.b - 1.f;
+    k.ab2 = 2.f * g.a * g.b;
     return k;
 }
 

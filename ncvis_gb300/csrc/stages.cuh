@@ -44,9 +44,12 @@ void launch_knn_select_f32(const float *Xp, const float *sqnorm, int64_t N, int 
                            const Segments &seg = Segments());
 int knn_f32_query_tile();
 // Exact distances of the candidates, top k+1 by (distance, index), smallest
-// dropped, k written in descending order: inds/dists [N, k].
+// dropped, k written in descending order: inds/dists [N, k].  `order` (a
+// permutation of the rows, or nullptr) is the order the rows are processed
+// in; the result does not depend on it.
 void launch_rerank(const float *Xp, int64_t N, int D, int dist, const int32_t *cand_i, int C,
-                   int k, int32_t *inds, float *dists, cudaStream_t s);
+                   int k, int32_t *inds, float *dists, cudaStream_t s,
+                   const int32_t *order = nullptr);
 
 // ---- K2 BF16 tensor-core candidate selection ---------------------------------
 struct KnnTcPlan {
@@ -118,7 +121,7 @@ void run_knn_tc_ordered(const float *Xp, const __nv_bfloat16 *Xb, const __nv_bfl
                         int64_t N, int D, const KnnTcPlan &tp, int dist, const KnnOrderPlan &op,
                         uint64_t seed, int32_t *cand_i, int *timeout_flag, cudaStream_t s,
                         void *workspace = nullptr, size_t workspace_bytes = 0,
-                        cudaEvent_t sweep_start = nullptr);
+                        cudaEvent_t sweep_start = nullptr, const int32_t **cell_order = nullptr);
 
 // Queries from Q (nq rows) against candidates from Cm (nc rows), both bf16
 // [rows, plan.ldb]; c_sqnorm: candidate squared norms (used for squared L2
