@@ -122,6 +122,13 @@ struct EpochConst {
     float b1, ab2;  // b - 1 and 2ab
 };
 
+// 2^x by the SFU's approximation (ex2.approx.ftz.f32, PTX ISA).
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // The update weight of one sample (w * step), Q copy updated in place.
 // With Ph = 1/denom, denom = 1 + a d2^b, nm = nu e^Q and t = 1 + nm denom:
 //   noise:    w = -1/t,      final weight -(2ab) d2^(b-1) / (t denom)
@@ -138,8 +145,8 @@ __device__ __forceinline__ float nce_weight(float d2, bool positive, const Epoch
     float p, p1;
     if (d2 > 0.f) {
         const float lg = __log2f(d2);
-        p = exp2f(__fmul_rn(k.b, lg));
-        p1 = exp2f(__fmul_rn(k.b1, lg));
+        p = ex2_approx(__fmul_rn(k.b, lg));
+        p1 = ex2_approx(__fmul_rn(k.b1, lg));
     } else {
         p = 0.f;
         p1 = k.pow_b1_at_zero;
