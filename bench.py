@@ -39,7 +39,7 @@ ONE_THREAD_N = 32_768  # points of the one-thread CPU figure
 RECALL_QUERIES = 10_000  # recall@15 sample against FP64 exact search
 # DRAM bytes (read + write) of one full-size BF16 kNN-selection launch, from a
 # one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum).
-KNN_TRAFFIC_BYTES = 9.60e9
+KNN_TRAFFIC_BYTES = 250.94e9
 
 
 def parse():
