@@ -615,8 +615,12 @@ __device__ __forceinline__ void gather_group(const float *Y, const int32_t (&sv)
 // group runs (one memory round trip per group instead of one per edge); a
 // gathered row that this chain wrote in between (an earlier positive row or
 // a stored source of the group) is read again, so the chain always sees its
-// own updates.
-template <int D, bool kWhole>
+// own updates.  kMulShift: every pick is a 32-bit Philox word scaled to the
+// window by multiply-shift (four per block; exactly uniform for any window
+// size W, as the window of a whole small problem needs; for a power of two it
+// takes the word's top bits); otherwise eight 16-bit halves of a block masked
+// to the power-of-two window.
+template <int D, bool kMulShift>
 __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict__ src,
                                              const int32_t *__restrict__ dst, int64_t a, int64_t b,
                                              const EpochConst &k, float &Qc, uint32_t key0,
@@ -663,9 +667,9 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
                     yi.v[c] = (yi.v[c] + dx) - dx;
                 }
             }
-            if constexpr (kWhole) {
-                // Whole-problem window of any size: the four 32-bit words of a
-                // Philox block give four picks by multiply-shift.
+            if constexpr (kMulShift) {
+                // The four 32-bit words of a Philox block give four picks by
+                // multiply-shift.
                 for (int s0 = 0; s0 < k.nu; s0 += 4) {
                     const Philox4x32 r = philox4x32_10((uint32_t)(e + q), (uint32_t)((e + q) >> 32),
                                                        tag, (uint32_t)(s0 >> 2) | 0x50000000u,
@@ -764,8 +768,9 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
 // Batched problems with staged noise: every block's chains belong to one
 // problem (problem p owns blocks [bp[p], bp[p+1]) and chains [cp[p], cp[p+1]),
 // the last block of a problem partly idle); the window is the problem's rows
-// when they fit (exact uniform picks over them) or 256-row segments at uniform
-// starts within the problem otherwise.  Blocks of T chains (T in 64, 128,
+// when they fit or 256-row segments at uniform starts within the problem
+// otherwise; either way each pick is a multiply-shift of a 32-bit Philox word
+// over the window, exactly uniform.  Blocks of T chains (T in 64, 128,
 // 256: the engine's autotuner picks T with the edges per chain).
 constexpr uint32_t kBatWindow = 1024;  // rows; two copies of d <= 4 floats fit 32 KB
 
@@ -812,12 +817,11 @@ __global__ void __launch_bounds__(T) sgd_epoch_window_batched(
         __syncthreads();
         const int64_t a = min(e1, e0 + (int64_t)r * round_edges);
         const int64_t b = min(e1, a + round_edges);
-        if (whole)
-            window_edges<D, true>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                                  have, ci, yi, yi0);
-        else
-            window_edges<D, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                                   have, ci, yi, yi0);
+        // One pick scheme for both window forms, so the kernel carries one copy
+        // of the edge loop (with two, its blocks of both forms on one SM
+        // thrashed the instruction cache).
+        window_edges<D, true>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws, have,
+                              ci, yi, yi0);
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < W; u += T) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);

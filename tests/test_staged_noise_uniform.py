@@ -3,8 +3,9 @@
 The staged kernels draw a round's noise samples from a window of Y instead of
 from all of it: 256-row segments at Philox-drawn uniform starts (wrapping at
 N), the window picks taken from 16-bit halves of one Philox block per eight
-samples, masked to the power-of-two window size; a problem that fits the
-batched kernel's window whole takes multiply-shift picks from 32-bit words.
+samples, masked to the power-of-two window size; the batched kernel takes
+multiply-shift picks from 32-bit words, over a whole small problem or over
+the segments of a larger one.
 Each sample is then uniform over the rows (before the redraw that skips the
 edge's source row).  These tests replay those exact draws (the Philox
 restatement of oracle/nce_oracle.py, vectorised) for independent samples and
@@ -24,11 +25,13 @@ def _chi2_ok(counts, expected):
     return abs(chi2 - dof) <= 6.0 * np.sqrt(2.0 * dof), chi2, dof
 
 
-def _segmented_rows(N, W, rounds, edges_per_round, seed, epoch, block=0):
+def _segmented_rows(N, W, rounds, edges_per_round, seed, epoch, block=0, mul_shift=False):
     """One noise sample per round: the first edge of round r, window pick
-    r mod 8 of its Philox block, through that round's segment starts.
-    Different rounds use disjoint Philox counters, so the samples are
-    independent; samples of one round share its window and are not."""
+    r mod 8 of its Philox block (mul_shift: word r mod 4 of the block scaled
+    to W by multiply-shift, the batched kernel's picks), through that round's
+    segment starts.  Different rounds use disjoint Philox counters, so the
+    samples are independent; samples of one round share its window and are
+    not."""
     k0, k1 = noise_key(seed)
     nseg = W // SEG
     r = np.arange(rounds, dtype=np.uint64)
@@ -38,11 +41,18 @@ def _segmented_rows(N, W, rounds, edges_per_round, seed, epoch, block=0):
                       t | np.uint64(0x20000000), (k0 ^ 0x3C6EF372) & 0xFFFFFFFF, k1)
     seg = bounded_index(x[0], x[1], N).reshape(rounds, nseg)
     e = r * np.uint64(edges_per_round)
-    b = philox4x32_10(e & MASK, e >> np.uint64(32), np.full(rounds, epoch, np.uint64),
-                      np.full(rounds, 0x40000000, np.uint64), k0, k1)
-    half = (r % np.uint64(8)).astype(np.int64)
-    word = np.stack(b)[half >> 1, np.arange(rounds)]
-    u = ((word >> (np.uint64(16) * (half & 1).astype(np.uint64))) & np.uint64(W - 1)).astype(np.int64)
+    if mul_shift:
+        b = philox4x32_10(e & MASK, e >> np.uint64(32), np.full(rounds, epoch, np.uint64),
+                          np.full(rounds, 0x50000000, np.uint64), k0, k1)
+        word = np.stack(b)[(r % np.uint64(4)).astype(np.int64), np.arange(rounds)]
+        u = ((word * np.uint64(W)) >> np.uint64(32)).astype(np.int64)
+    else:
+        b = philox4x32_10(e & MASK, e >> np.uint64(32), np.full(rounds, epoch, np.uint64),
+                          np.full(rounds, 0x40000000, np.uint64), k0, k1)
+        half = (r % np.uint64(8)).astype(np.int64)
+        word = np.stack(b)[half >> 1, np.arange(rounds)]
+        u = ((word >> (np.uint64(16) * (half & 1).astype(np.uint64))) &
+             np.uint64(W - 1)).astype(np.int64)
     rows = seg[np.arange(rounds), u // SEG] + u % SEG
     return np.where(rows >= N, rows - N, rows)
 
@@ -59,6 +69,17 @@ def test_segmented_window_rows_are_uniform_when_n_is_not_a_multiple():
     # N not a multiple of the segment length: segments wrap at N.
     N, W = 20011, 1024
     rows = _segmented_rows(N, W, rounds=N * 24, edges_per_round=64, seed=3, epoch=1)
+    counts = np.bincount(rows, minlength=N).astype(np.float64)
+    ok, chi2, dof = _chi2_ok(counts, rows.size / N)
+    assert ok, (chi2, dof)
+
+
+def test_batched_segmented_window_rows_are_uniform():
+    # Batched problems larger than the window: 256-row segments of the
+    # problem, picks by multiply-shift of 32-bit words over the 1,024 rows.
+    N, W = 20011, 1024
+    rows = _segmented_rows(N, W, rounds=N * 24, edges_per_round=64, seed=9, epoch=4, block=3,
+                           mul_shift=True)
     counts = np.bincount(rows, minlength=N).astype(np.float64)
     ok, chi2, dof = _chi2_ok(counts, rows.size / N)
     assert ok, (chi2, dof)
