@@ -14,25 +14,34 @@
 //   1. count_targets / scan: in-degree of every row and bucket offsets;
 //   2. scatter_incoming: each table entry e = s*k + j appends e to its
 //      target's bucket (atomic cursor; arrival order is not deterministic);
-//   3. merge_rows, one thread per row: sorts its bucket by e, which restores
-//      the one-thread arrival order, builds the row's (distance, position)
-//      items, runs the libstdc++-equivalent introsort (introsort.cuh) and the
-//      in-place deduplication; rows of up to kCap items live in shared
-//      memory, longer rows in a row-aligned global scratch;
+//   3. merge, one thread per row (merge_row.cuh): sorts its bucket by e,
+//      which restores the one-thread arrival order, builds the row's
+//      (distance, position) items, runs the libstdc++-equivalent introsort
+//      (introsort.cuh) and the in-place deduplication, all in the thread's
+//      slots of shared memory.  Rows go through tiers of growing capacity:
+//      every row starts in merge_tier<48> (k + in-degree is ~30 on average);
+//      a row that does not fit is appended to the next tier's list
+//      (merge_tier<128>, then merge_tier<320>); the few rows longer than the
+//      last tier run on a row-aligned global scratch;
 //   4. scan of the kept counts -> row_ptr; compact_rows writes cols, vals and
 //      the source row of every entry (the build_edges pairs).
 #include <algorithm>
 
 #include "common.cuh"
 #include "introsort.cuh"
+#include "merge_row.cuh"
 #include "stages.cuh"
 
 namespace ncvis_gpu {
 
 namespace {
 
-constexpr int kCap = 64;         // row items held in shared memory per thread
-constexpr int kMergeThreads = 128;
+// Merge tiers: items per row held in shared memory (12 B each: the sort item
+// and the row's index at that position) and threads per block; each tier's
+// blocks fit 3, 2 and 1 times per SM.
+constexpr int kCap0 = 48, kThreads0 = 128;
+constexpr int kCap1 = 128, kThreads1 = 64;
+constexpr int kCap2 = 320, kThreads2 = 32;
 
 // Flags any index outside [0, N) (the table must name existing points).
 __global__ void check_indices(const int32_t *__restrict__ inds, int64_t nk, int64_t N,
@@ -73,52 +82,6 @@ __global__ void scatter_incoming(const int32_t *__restrict__ inds, int64_t nk,
     }
 }
 
-// Ascending sort of distinct integers (a row's incoming entry ids).
-__device__ void sort_distinct(int32_t *a, int n) {
-    if (n <= 32) {
-        for (int i = 1; i < n; ++i) {
-            int32_t v = a[i];
-            int j = i - 1;
-            while (j >= 0 && a[j] > v) {
-                a[j + 1] = a[j];
-                --j;
-            }
-            a[j + 1] = v;
-        }
-        return;
-    }
-    // heap sort
-    for (int start = n / 2 - 1; start >= 0; --start) {
-        int root = start;
-        for (;;) {
-            int child = 2 * root + 1;
-            if (child >= n) break;
-            if (child + 1 < n && a[child] < a[child + 1]) ++child;
-            if (a[root] >= a[child]) break;
-            int32_t t = a[root];
-            a[root] = a[child];
-            a[child] = t;
-            root = child;
-        }
-    }
-    for (int end = n - 1; end > 0; --end) {
-        int32_t t = a[0];
-        a[0] = a[end];
-        a[end] = t;
-        int root = 0;
-        for (;;) {
-            int child = 2 * root + 1;
-            if (child >= end) break;
-            if (child + 1 < end && a[child] < a[child + 1]) ++child;
-            if (a[root] >= a[child]) break;
-            int32_t u = a[root];
-            a[root] = a[child];
-            a[child] = u;
-            root = child;
-        }
-    }
-}
-
 template <class V>
 __device__ __forceinline__ int32_t merge_one(V items, int L, int k, const int32_t *__restrict__ own_i,
                                              const float *__restrict__ own_d,
@@ -149,29 +112,72 @@ __device__ __forceinline__ int32_t merge_one(V items, int L, int k, const int32_
     return n_out;
 }
 
-__global__ void __launch_bounds__(kMergeThreads) merge_rows(
-    int64_t N, int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
-    const int64_t *__restrict__ in_off, int32_t *__restrict__ in_key, SortItem *__restrict__ g_items,
-    int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept) {
-    extern __shared__ __align__(16) SortItem sm_items[];  // [kCap][kMergeThreads]
-    const int64_t i = (int64_t)blockIdx.x * kMergeThreads + threadIdx.x;
-    if (i >= N) return;
+// Rows whose k + in-degree exceeds every tier: the row-aligned global scratch.
+__device__ int32_t merge_global(int64_t i, int k, const int32_t *__restrict__ inds,
+                                const float *__restrict__ dists, const int64_t *__restrict__ in_off,
+                                int32_t *__restrict__ in_key, SortItem *__restrict__ g_items,
+                                int32_t *__restrict__ out_col, float *__restrict__ out_val) {
     const int64_t ib = in_off[i];
     const int nin = (int)(in_off[i + 1] - ib);
-    const int L = k + nin;
-    const int64_t base = i * k + ib;  // row-aligned scratch offset
+    const int64_t base = i * k + ib;
     int32_t *ink = in_key + ib;
-    sort_distinct(ink, nin);
-    int32_t n;
-    if (L <= kCap) {
-        StridedItems view{sm_items + threadIdx.x, kMergeThreads};
-        n = merge_one(view, L, k, inds + i * k, dists + i * k, ink, dists, out_col + base,
-                      out_val + base);
-    } else {
-        n = merge_one(g_items + base, L, k, inds + i * k, dists + i * k, ink, dists,
-                      out_col + base, out_val + base);
+    sort_distinct_ints(ink, 0, nin);
+    return merge_one(g_items + base, k + nin, k, inds + i * k, dists + i * k, ink, dists,
+                     out_col + base, out_val + base);
+}
+
+// One merge tier.  Its rows are 0 .. N-1 (rows == null) or rows[0 .. *n_rows);
+// a row of more than C items is appended to next (or, in the last tier, run
+// on the global scratch).  Shared memory: [C][T] sort items, then [C][T]
+// indices; thread t's slot i of either is element i * T + t.
+template <int C, int T>
+__global__ void __launch_bounds__(T) merge_tier(
+    int64_t N, int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
+    const int64_t *__restrict__ in_off, int32_t *__restrict__ in_key, SortItem *__restrict__ g_items,
+    int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept,
+    const int32_t *__restrict__ rows, const int32_t *__restrict__ n_rows, int32_t *__restrict__ next,
+    int32_t *__restrict__ n_next) {
+    extern __shared__ __align__(16) SortItem sm_items[];
+    int32_t *sm_orig = reinterpret_cast<int32_t *>(sm_items + C * T);
+    const int64_t count = rows ? (int64_t)*n_rows : N;
+    for (int64_t w = (int64_t)blockIdx.x * T + threadIdx.x; w < count; w += (int64_t)gridDim.x * T) {
+        const int64_t i = rows ? (int64_t)rows[w] : w;
+        const int64_t ib = in_off[i];
+        const int nin = (int)(in_off[i + 1] - ib);
+        const int L = k + nin;
+        const int64_t base = i * k + ib;  // row-aligned output offset
+        if (L > C) {
+            if (next)
+                next[atomicAdd(n_next, 1)] = (int32_t)i;
+            else
+                kept[i] = merge_global(i, k, inds, dists, in_off, in_key, g_items, out_col, out_val);
+            continue;
+        }
+        StridedItems items{sm_items + threadIdx.x, T};
+        StridedInts orig{sm_orig + threadIdx.x, T};
+        const int32_t *ink = in_key + ib;
+        for (int q = 0; q < nin; ++q) orig[k + q] = ink[q];
+        kept[i] = merge_row(items, orig, L, k, inds + i * k, dists + i * k, dists, out_col + base,
+                            out_val + base);
     }
-    kept[i] = n;
+}
+
+template <int C, int T>
+void launch_merge_tier(int64_t N, int k, const int32_t *inds, const float *dists,
+                       const int64_t *in_off, int32_t *in_key, SortItem *g_items, int32_t *out_col,
+                       float *out_val, int32_t *kept, const int32_t *rows, const int32_t *n_rows,
+                       int32_t *next, int32_t *n_next, cudaStream_t s) {
+    const size_t smem = (sizeof(SortItem) + sizeof(int32_t)) * C * T;
+    // Set on every launch: the attribute is per device, and a cached flag
+    // would race between host threads running different engines.
+    NCVIS_CUDA(cudaFuncSetAttribute(merge_tier<C, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    // All rows: one thread each; listed rows: a grid of resident blocks that
+    // reads the list's length on the device.
+    const int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
+    const int64_t grid = rows ? (int64_t)num_sms() * per_sm : ceil_div(N, T);
+    NCVIS_LAUNCH((merge_tier<C, T>), grid, T, smem, s, N, k, inds, dists, in_off, in_key, g_items,
+                 out_col, out_val, kept, rows, n_rows, next, n_next);
 }
 
 __global__ void compact_rows(int64_t N, int k, const int64_t *__restrict__ in_off,
@@ -193,7 +199,7 @@ __global__ void compact_rows(int64_t N, int k, const int64_t *__restrict__ in_of
 }
 
 struct SymWs {
-    int32_t *indeg, *cursor, *in_key, *out_col, *kept, *bad;
+    int32_t *indeg, *cursor, *in_key, *out_col, *kept, *bad, *tier1, *tier2, *n_tier;
     int64_t *in_off;
     SortItem *items;
     float *out_val;
@@ -210,6 +216,9 @@ SymWs carve(void *ws, int64_t N, int k) {
     w.cursor = (int32_t *)p;   p += align256(sizeof(int32_t) * N);
     w.kept = (int32_t *)p;     p += align256(sizeof(int32_t) * N);
     w.bad = (int32_t *)p;      p += align256(sizeof(int32_t));
+    w.n_tier = (int32_t *)p;   p += align256(2 * sizeof(int32_t));
+    w.tier1 = (int32_t *)p;    p += align256(sizeof(int32_t) * N);
+    w.tier2 = (int32_t *)p;    p += align256(sizeof(int32_t) * N);
     w.in_off = (int64_t *)p;   p += align256(sizeof(int64_t) * (N + 1));
     w.in_key = (int32_t *)p;   p += align256(sizeof(int32_t) * nk);
     w.items = (SortItem *)p;   p += align256(sizeof(SortItem) * 2 * nk);
@@ -241,7 +250,8 @@ bool edges_in_range(const int32_t *a, const int32_t *b, int64_t n, int64_t N, cu
 
 size_t symmetrize_workspace_bytes(int64_t N, int k) {
     const int64_t nk = N * k;
-    return 3 * align256(sizeof(int32_t) * N) + align256(sizeof(int32_t)) +
+    return 5 * align256(sizeof(int32_t) * N) + align256(sizeof(int32_t)) +
+           align256(2 * sizeof(int32_t)) +
            align256(sizeof(int64_t) * (N + 1)) +
            align256(sizeof(int32_t) * nk) + align256(sizeof(SortItem) * 2 * nk) +
            align256(sizeof(int32_t) * 2 * nk) + align256(sizeof(float) * 2 * nk) +
@@ -267,13 +277,15 @@ int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists
     NCVIS_LAUNCH(count_targets, grid, 256, 0, s, inds, nk, w.indeg);
     launch_exclusive_scan_i32_to_i64(w.indeg, w.in_off, N, w.scan, s);
     NCVIS_LAUNCH(scatter_incoming, grid, 256, 0, s, inds, nk, w.in_off, w.cursor, w.in_key);
-    const size_t smem = sizeof(SortItem) * kCap * kMergeThreads;
-    // Set on every launch: the attribute is per device, and a cached flag
-    // would race between host threads running different engines.
-    NCVIS_CUDA(cudaFuncSetAttribute(merge_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    NCVIS_LAUNCH(merge_rows, ceil_div(N, kMergeThreads), kMergeThreads, smem, s, N, k, inds, dists,
-                 w.in_off, w.in_key, w.items, w.out_col, w.out_val, w.kept);
+    NCVIS_CUDA(cudaMemsetAsync(w.n_tier, 0, 2 * sizeof(int32_t), s));
+    launch_merge_tier<kCap0, kThreads0>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                        w.out_val, w.kept, nullptr, nullptr, w.tier1, w.n_tier, s);
+    launch_merge_tier<kCap1, kThreads1>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                        w.out_val, w.kept, w.tier1, w.n_tier, w.tier2,
+                                        w.n_tier + 1, s);
+    launch_merge_tier<kCap2, kThreads2>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                        w.out_val, w.kept, w.tier2, w.n_tier + 1, nullptr, nullptr,
+                                        s);
     launch_exclusive_scan_i32_to_i64(w.kept, row_ptr, N, w.scan, s);
     NCVIS_LAUNCH(compact_rows, ceil_div(N, 8), 256, 0, s, N, k, w.in_off, w.kept, row_ptr,
                  w.out_col, w.out_val, cols, vals, src);

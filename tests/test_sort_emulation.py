@@ -23,3 +23,20 @@ def test_introsort_matches_std_sort(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok "), r.stdout
     assert int(r.stdout.split()[1]) >= 20000
+
+
+def test_staged_row_merge_matches_reference_steps(tmp_path):
+    """The staged row merge (ncvis_gb300/csrc/merge_row.cuh, the per-row body
+    of the GPU symmetrization) against a direct statement of the reference's
+    append order, index sort and in-place deduplication
+    (src/knntable.cpp:40-49, 81-93), over plain arrays and over strided
+    views like the GPU's shared-memory rows (tests/harness/merge_check.cpp)."""
+    src = os.path.join(ROOT, "tests", "harness", "merge_check.cpp")
+    exe = str(tmp_path / "merge_check")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "ncvis_gb300", "csrc"),
+                        src, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe, "20000"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok "), r.stdout
+    assert int(r.stdout.split()[1]) >= 20000
