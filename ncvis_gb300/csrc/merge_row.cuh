@@ -3,9 +3,11 @@
 // KNNTable::symmetrize for row i (src/knntable.cpp:60-96) on the row's own k
 // table entries and its incoming entries.
 //
-// Inputs: orig[k, L) holds the row's incoming entry ids e = s*k + j (any
-// order, distinct); own_i / own_d are the row's k table entries; dists is the
-// whole table's distances (the incoming entry e carries dists[e]).
+// Inputs: ink[0, L - k) the row's incoming entry ids e = s*k + j (any order,
+// distinct); own_i / own_d the row's k table entries; dists the whole table's
+// distances (the incoming entry e carries dists[e]).  items and orig provide
+// L slots each.  Global loads are issued four at a time, so a row waits for
+// about a quarter of its entries' round trips.
 // Steps:
 //   * the incoming ids are sorted ascending, which is the order one thread
 //     appends them in (src/knntable.cpp:40-49);
@@ -73,21 +75,11 @@ NCVIS_HD void sort_distinct_ints(V a, int32_t off, int32_t n) {
     }
 }
 
+// The sort and the deduplication of a built row (items[p] = (distance at p,
+// p), orig[p] = index at p): afterwards items[0, n_out) are the kept items in
+// order, their indices orig[items[q].pos].  Returns n_out.
 template <class VI, class VO>
-NCVIS_HD int32_t merge_row(VI items, VO orig, int32_t L, int32_t k,
-                           const int32_t *__restrict__ own_i, const float *__restrict__ own_d,
-                           const float *__restrict__ dists, int32_t *__restrict__ out_col,
-                           float *__restrict__ out_val) {
-    sort_distinct_ints(orig, k, L - k);
-    for (int32_t p = 0; p < k; ++p) {
-        items[p] = SortItem{own_d[p], p};
-        orig[p] = own_i[p];
-    }
-    for (int32_t p = k; p < L; ++p) {
-        const int32_t e = orig[p];
-        items[p] = SortItem{dists[e], p};
-        orig[p] = e / k;
-    }
+NCVIS_HD int32_t sort_and_dedup(VI items, VO orig, int32_t L) {
     libstdcxx_sort(items, L);
     int32_t n_out = 0;
     for (int32_t j = 0; j < L; ++j) {
@@ -101,6 +93,42 @@ NCVIS_HD int32_t merge_row(VI items, VO orig, int32_t L, int32_t k,
         }
         if (keep) items[n_out++] = cur;
     }
+    return n_out;
+}
+
+template <class VI, class VO>
+NCVIS_HD int32_t merge_row(VI items, VO orig, int32_t L, int32_t k,
+                           const int32_t *__restrict__ own_i, const float *__restrict__ own_d,
+                           const int32_t *__restrict__ ink, const float *__restrict__ dists,
+                           int32_t *__restrict__ out_col, float *__restrict__ out_val) {
+    int32_t p = k;
+    for (; p + 4 <= L; p += 4) {
+        int32_t e[4];
+        for (int u = 0; u < 4; ++u) e[u] = ink[p - k + u];
+        for (int u = 0; u < 4; ++u) orig[p + u] = e[u];
+    }
+    for (; p < L; ++p) orig[p] = ink[p - k];
+    sort_distinct_ints(orig, k, L - k);
+    for (p = 0; p + 4 <= k; p += 4) {
+        int32_t c[4];
+        float d[4];
+        for (int u = 0; u < 4; ++u) c[u] = own_i[p + u], d[u] = own_d[p + u];
+        for (int u = 0; u < 4; ++u) items[p + u] = SortItem{d[u], p + u}, orig[p + u] = c[u];
+    }
+    for (; p < k; ++p) items[p] = SortItem{own_d[p], p}, orig[p] = own_i[p];
+    for (; p + 4 <= L; p += 4) {
+        int32_t e[4];
+        float d[4];
+        for (int u = 0; u < 4; ++u) e[u] = orig[p + u];
+        for (int u = 0; u < 4; ++u) d[u] = dists[e[u]];
+        for (int u = 0; u < 4; ++u) items[p + u] = SortItem{d[u], p + u}, orig[p + u] = e[u] / k;
+    }
+    for (; p < L; ++p) {
+        const int32_t e = orig[p];
+        items[p] = SortItem{dists[e], p};
+        orig[p] = e / k;
+    }
+    const int32_t n_out = sort_and_dedup(items, orig, L);
     for (int32_t q = 0; q < n_out; ++q) {
         const SortItem it = items[q];
         out_col[q] = orig[it.pos];

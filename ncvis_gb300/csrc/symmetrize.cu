@@ -18,11 +18,10 @@
 //      which restores the one-thread arrival order, builds the row's
 //      (distance, position) items, runs the libstdc++-equivalent introsort
 //      (introsort.cuh) and the in-place deduplication, all in the thread's
-//      slots of shared memory.  Rows go through tiers of growing capacity:
-//      every row starts in merge_tier<48> (k + in-degree is ~30 on average);
-//      a row that does not fit is appended to the next tier's list
-//      (merge_tier<128>, then merge_tier<320>); the few rows longer than the
-//      last tier run on a row-aligned global scratch;
+//      slots of shared memory (merge_rows_thread, rows of up to 48 items);
+//      longer rows are listed and merged one warp per row (merge_rows_warp,
+//      tiers of 128, 1,024 and 8,192 items), longer still on a row-aligned
+//      global scratch;
 //   4. scan of the kept counts -> row_ptr; compact_rows writes cols, vals and
 //      the source row of every entry (the build_edges pairs).
 #include <algorithm>
@@ -36,12 +35,16 @@ namespace ncvis_gpu {
 
 namespace {
 
-// Merge tiers: items per row held in shared memory (12 B each: the sort item
-// and the row's index at that position) and threads per block; each tier's
-// blocks fit 3, 2 and 1 times per SM.
+// Merge tiers by row length k + in-degree (~30 on average): up to 48 items
+// one thread per row (12 B per item in shared memory: the sort item and the
+// row's index at that position; 3 blocks of 128 threads per SM); longer rows
+// one warp per row, in tiers of 128, 1,024 and 8,192 items (hubs: rows of up
+// to ~1,000 items occur in 64-dimensional mixtures of a few thousand points);
+// longer still on the global scratch.
 constexpr int kCap0 = 48, kThreads0 = 128;
-constexpr int kCap1 = 128, kThreads1 = 64;
-constexpr int kCap2 = 320, kThreads2 = 32;
+constexpr int kCap1 = 128, kWarps1 = 8;
+constexpr int kCap2 = 1024, kWarps2 = 4;
+constexpr int kCap3 = 8192, kWarps3 = 1;
 
 // Flags any index outside [0, N) (the table must name existing points).
 __global__ void check_indices(const int32_t *__restrict__ inds, int64_t nk, int64_t N,
@@ -126,58 +129,130 @@ __device__ int32_t merge_global(int64_t i, int k, const int32_t *__restrict__ in
                      out_col + base, out_val + base);
 }
 
-// One merge tier.  Its rows are 0 .. N-1 (rows == null) or rows[0 .. *n_rows);
-// a row of more than C items is appended to next (or, in the last tier, run
-// on the global scratch).  Shared memory: [C][T] sort items, then [C][T]
-// indices; thread t's slot i of either is element i * T + t.
+// First tier: every row, one thread each; its items live in the thread's
+// slots of shared memory ([C][T] sort items, then [C][T] indices; slot i of
+// thread t is element i * T + t).  A row of more than C items is appended to
+// `next` for the warp tiers.
 template <int C, int T>
-__global__ void __launch_bounds__(T) merge_tier(
+__global__ void __launch_bounds__(T, 1) merge_rows_thread(
     int64_t N, int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
+    const int64_t *__restrict__ in_off, const int32_t *__restrict__ in_key,
+    int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept,
+    int32_t *__restrict__ next, int32_t *__restrict__ n_next) {
+    extern __shared__ __align__(16) SortItem sm_items[];
+    int32_t *sm_orig = reinterpret_cast<int32_t *>(sm_items + C * T);
+    const int64_t i = (int64_t)blockIdx.x * T + threadIdx.x;
+    if (i >= N) return;
+    const int64_t ib = in_off[i];
+    const int nin = (int)(in_off[i + 1] - ib);
+    const int L = k + nin;
+    if (L > C) {
+        next[atomicAdd(n_next, 1)] = (int32_t)i;
+        return;
+    }
+    const int64_t base = i * k + ib;  // row-aligned output offset
+    StridedItems items{sm_items + threadIdx.x, T};
+    StridedInts orig{sm_orig + threadIdx.x, T};
+    kept[i] = merge_row(items, orig, L, k, inds + i * k, dists + i * k, in_key + ib, dists,
+                        out_col + base, out_val + base);
+}
+
+// Warp tiers: the listed rows rows[0 .. *n_rows), one warp each (W warps per
+// block, C items per warp in shared memory: [W][C] sort items, then [W][C]
+// indices).  Long rows are rare, and one thread per row would leave a warp
+// running 32 of them one after the other through divergent sorts.  The warp
+// loads the row, sorts its incoming ids (each id's rank among the row's ids;
+// the ids are distinct) and gathers the distances in parallel; lane 0 runs
+// the sort and the deduplication (sequential: the tie order is
+// libstdc++'s); the warp writes the kept entries.  A row of more than C
+// items goes to `next`, or, in the last tier, to the global scratch.
+template <int C, int W>
+__global__ void __launch_bounds__(32 * W, 1) merge_rows_warp(
+    int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
     const int64_t *__restrict__ in_off, int32_t *__restrict__ in_key, SortItem *__restrict__ g_items,
     int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept,
     const int32_t *__restrict__ rows, const int32_t *__restrict__ n_rows, int32_t *__restrict__ next,
     int32_t *__restrict__ n_next) {
     extern __shared__ __align__(16) SortItem sm_items[];
-    int32_t *sm_orig = reinterpret_cast<int32_t *>(sm_items + C * T);
-    const int64_t count = rows ? (int64_t)*n_rows : N;
-    for (int64_t w = (int64_t)blockIdx.x * T + threadIdx.x; w < count; w += (int64_t)gridDim.x * T) {
-        const int64_t i = rows ? (int64_t)rows[w] : w;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    SortItem *items = sm_items + (size_t)warp * C;
+    int32_t *orig = reinterpret_cast<int32_t *>(sm_items + (size_t)W * C) + (size_t)warp * C;
+    int32_t *sorted_ids = reinterpret_cast<int32_t *>(items);  // 2C ints before the items exist
+    const int64_t count = *n_rows;
+    for (int64_t w = (int64_t)blockIdx.x * W + warp; w < count; w += (int64_t)gridDim.x * W) {
+        const int64_t i = rows[w];
         const int64_t ib = in_off[i];
         const int nin = (int)(in_off[i + 1] - ib);
         const int L = k + nin;
         const int64_t base = i * k + ib;  // row-aligned output offset
         if (L > C) {
-            if (next)
-                next[atomicAdd(n_next, 1)] = (int32_t)i;
-            else
-                kept[i] = merge_global(i, k, inds, dists, in_off, in_key, g_items, out_col, out_val);
+            if (lane == 0) {
+                if (next)
+                    next[atomicAdd(n_next, 1)] = (int32_t)i;
+                else
+                    kept[i] = merge_global(i, k, inds, dists, in_off, in_key, g_items, out_col,
+                                           out_val);
+            }
             continue;
         }
-        StridedItems items{sm_items + threadIdx.x, T};
-        StridedInts orig{sm_orig + threadIdx.x, T};
         const int32_t *ink = in_key + ib;
-        for (int q = 0; q < nin; ++q) orig[k + q] = ink[q];
-        kept[i] = merge_row(items, orig, L, k, inds + i * k, dists + i * k, dists, out_col + base,
-                            out_val + base);
+        for (int q = lane; q < nin; q += 32) orig[k + q] = ink[q];
+        __syncwarp();
+        for (int q = lane; q < nin; q += 32) {
+            const int32_t e = orig[k + q];
+            int r = 0;
+            for (int t = 0; t < nin; ++t) r += orig[k + t] < e;
+            sorted_ids[r] = e;
+        }
+        __syncwarp();
+        for (int q = lane; q < nin; q += 32) orig[k + q] = sorted_ids[q];
+        __syncwarp();
+        for (int p = lane; p < L; p += 32) {
+            if (p < k) {
+                items[p] = SortItem{dists[i * k + p], p};
+                orig[p] = inds[i * k + p];
+            } else {
+                const int32_t e = orig[p];
+                items[p] = SortItem{dists[e], p};
+                orig[p] = e / k;
+            }
+        }
+        __syncwarp();
+        int32_t n_out = 0;
+        if (lane == 0) n_out = sort_and_dedup(items, orig, L);
+        n_out = __shfl_sync(0xffffffffu, n_out, 0);
+        __syncwarp();
+        for (int q = lane; q < n_out; q += 32) {
+            const SortItem it = items[q];
+            out_col[base + q] = orig[it.pos];
+            out_val[base + q] = it.key;
+        }
+        if (lane == 0) kept[i] = n_out;
+        __syncwarp();
     }
 }
 
-template <int C, int T>
-void launch_merge_tier(int64_t N, int k, const int32_t *inds, const float *dists,
-                       const int64_t *in_off, int32_t *in_key, SortItem *g_items, int32_t *out_col,
-                       float *out_val, int32_t *kept, const int32_t *rows, const int32_t *n_rows,
-                       int32_t *next, int32_t *n_next, cudaStream_t s) {
-    const size_t smem = (sizeof(SortItem) + sizeof(int32_t)) * C * T;
+// Blocks per SM for a block of `threads` threads and `smem` bytes of shared
+// memory (the warp tiers use 64 registers per thread: 1,024 threads per SM).
+inline int blocks_per_sm(size_t smem, int threads) {
+    const int by_smem = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
+    return std::max(1, std::min(by_smem, 1024 / threads));
+}
+
+template <int C, int W>
+void launch_merge_warp(int k, const int32_t *inds, const float *dists, const int64_t *in_off,
+                       int32_t *in_key, SortItem *g_items, int32_t *out_col, float *out_val,
+                       int32_t *kept, const int32_t *rows, const int32_t *n_rows, int32_t *next,
+                       int32_t *n_next, cudaStream_t s) {
+    const size_t smem = (sizeof(SortItem) + sizeof(int32_t)) * C * W;
     // Set on every launch: the attribute is per device, and a cached flag
     // would race between host threads running different engines.
-    NCVIS_CUDA(cudaFuncSetAttribute(merge_tier<C, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    // All rows: one thread each; listed rows: a grid of resident blocks that
-    // reads the list's length on the device.
-    const int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
-    const int64_t grid = rows ? (int64_t)num_sms() * per_sm : ceil_div(N, T);
-    NCVIS_LAUNCH((merge_tier<C, T>), grid, T, smem, s, N, k, inds, dists, in_off, in_key, g_items,
-                 out_col, out_val, kept, rows, n_rows, next, n_next);
+    NCVIS_CUDA(cudaFuncSetAttribute(merge_rows_warp<C, W>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // A grid of resident blocks that reads the list's length on the device.
+    const int64_t grid = (int64_t)num_sms() * blocks_per_sm(smem, 32 * W);
+    NCVIS_LAUNCH((merge_rows_warp<C, W>), grid, 32 * W, smem, s, k, inds, dists, in_off, in_key,
+                 g_items, out_col, out_val, kept, rows, n_rows, next, n_next);
 }
 
 __global__ void compact_rows(int64_t N, int k, const int64_t *__restrict__ in_off,
@@ -216,7 +291,7 @@ SymWs carve(void *ws, int64_t N, int k) {
     w.cursor = (int32_t *)p;   p += align256(sizeof(int32_t) * N);
     w.kept = (int32_t *)p;     p += align256(sizeof(int32_t) * N);
     w.bad = (int32_t *)p;      p += align256(sizeof(int32_t));
-    w.n_tier = (int32_t *)p;   p += align256(2 * sizeof(int32_t));
+    w.n_tier = (int32_t *)p;   p += align256(3 * sizeof(int32_t));
     w.tier1 = (int32_t *)p;    p += align256(sizeof(int32_t) * N);
     w.tier2 = (int32_t *)p;    p += align256(sizeof(int32_t) * N);
     w.in_off = (int64_t *)p;   p += align256(sizeof(int64_t) * (N + 1));
@@ -251,7 +326,7 @@ bool edges_in_range(const int32_t *a, const int32_t *b, int64_t n, int64_t N, cu
 size_t symmetrize_workspace_bytes(int64_t N, int k) {
     const int64_t nk = N * k;
     return 5 * align256(sizeof(int32_t) * N) + align256(sizeof(int32_t)) +
-           align256(2 * sizeof(int32_t)) +
+           align256(3 * sizeof(int32_t)) +
            align256(sizeof(int64_t) * (N + 1)) +
            align256(sizeof(int32_t) * nk) + align256(sizeof(SortItem) * 2 * nk) +
            align256(sizeof(int32_t) * 2 * nk) + align256(sizeof(float) * 2 * nk) +
@@ -277,15 +352,24 @@ int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists
     NCVIS_LAUNCH(count_targets, grid, 256, 0, s, inds, nk, w.indeg);
     launch_exclusive_scan_i32_to_i64(w.indeg, w.in_off, N, w.scan, s);
     NCVIS_LAUNCH(scatter_incoming, grid, 256, 0, s, inds, nk, w.in_off, w.cursor, w.in_key);
-    NCVIS_CUDA(cudaMemsetAsync(w.n_tier, 0, 2 * sizeof(int32_t), s));
-    launch_merge_tier<kCap0, kThreads0>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
-                                        w.out_val, w.kept, nullptr, nullptr, w.tier1, w.n_tier, s);
-    launch_merge_tier<kCap1, kThreads1>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
-                                        w.out_val, w.kept, w.tier1, w.n_tier, w.tier2,
-                                        w.n_tier + 1, s);
-    launch_merge_tier<kCap2, kThreads2>(N, k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
-                                        w.out_val, w.kept, w.tier2, w.n_tier + 1, nullptr, nullptr,
-                                        s);
+    NCVIS_CUDA(cudaMemsetAsync(w.n_tier, 0, 3 * sizeof(int32_t), s));
+    {
+        const size_t smem = (sizeof(SortItem) + sizeof(int32_t)) * kCap0 * kThreads0;
+        NCVIS_CUDA(cudaFuncSetAttribute(merge_rows_thread<kCap0, kThreads0>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCVIS_LAUNCH((merge_rows_thread<kCap0, kThreads0>), ceil_div(N, kThreads0), kThreads0,
+                     smem, s, N, k, inds, dists, w.in_off, w.in_key, w.out_col, w.out_val, w.kept,
+                     w.tier1, w.n_tier);
+    }
+    launch_merge_warp<kCap1, kWarps1>(k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                      w.out_val, w.kept, w.tier1, w.n_tier, w.tier2, w.n_tier + 1,
+                                      s);
+    launch_merge_warp<kCap2, kWarps2>(k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                      w.out_val, w.kept, w.tier2, w.n_tier + 1, w.tier1,
+                                      w.n_tier + 2, s);
+    launch_merge_warp<kCap3, kWarps3>(k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
+                                      w.out_val, w.kept, w.tier1, w.n_tier + 2, nullptr, nullptr,
+                                      s);
     launch_exclusive_scan_i32_to_i64(w.kept, row_ptr, N, w.scan, s);
     NCVIS_LAUNCH(compact_rows, ceil_div(N, 8), 256, 0, s, N, k, w.in_off, w.kept, row_ptr,
                  w.out_col, w.out_val, cols, vals, src);

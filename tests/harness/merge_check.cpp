@@ -85,16 +85,16 @@ int main(int argc, char **argv) {
             std::vector<float> got_v(L, -7.f);
             int32_t ng;
             if (form == 0) {
-                for (int32_t q = 0; q < m; ++q) og_store[k + q] = in_ids[q];
                 ng = ncvis_gpu::merge_row(it_store.data(), og_store.data(), L, k, own_i.data(),
-                                          own_d.data(), table_d.data(), got_c.data(), got_v.data());
+                                          own_d.data(), in_ids.data(), table_d.data(),
+                                          got_c.data(), got_v.data());
             } else {
                 const int lane = r % stride;
                 ncvis_gpu::StridedItems items{it_store.data() + lane, stride};
                 ncvis_gpu::StridedInts orig{og_store.data() + lane, stride};
-                for (int32_t q = 0; q < m; ++q) orig[k + q] = in_ids[q];
                 ng = ncvis_gpu::merge_row(items, orig, L, k, own_i.data(), own_d.data(),
-                                          table_d.data(), got_c.data(), got_v.data());
+                                          in_ids.data(), table_d.data(), got_c.data(),
+                                          got_v.data());
             }
             bool same = ng == nw;
             for (int32_t q = 0; same && q < nw; ++q)

@@ -62,7 +62,7 @@ def test_tie_heavy(cuda, oracle, seed, N, k, levels):
 
 
 def test_hubs_long_rows(cuda, oracle):
-    """Rows with hundreds of entries take the global-memory path."""
+    """Rows with over a thousand entries (hubs)."""
     rng = np.random.default_rng(7)
     N, k = 6000, 15
     hubs = rng.integers(0, N, size=20)
@@ -72,6 +72,35 @@ def test_hubs_long_rows(cuda, oracle):
     dists = -np.sort(-dists, axis=1)
     rp, cols, vals = oracle.symmetrize(inds, dists)
     assert np.diff(rp).max() > 200
+    _assert_same(_gpu_sym(cuda, inds, dists), rp, cols, vals)
+
+
+def test_rows_across_merge_tiers(cuda, oracle):
+    """Row lengths k + in-degree in every merge tier of the GPU path (up to 48
+    items one thread per row; 128, 1,024 and 8,192 items one warp per row;
+    longer on the global scratch), with tied distances."""
+    rng = np.random.default_rng(11)
+    N, k = 30000, 15
+    inds = rng.integers(0, N - 1, size=(N, k))
+    inds = inds + (inds >= np.arange(N)[:, None])  # no self entries
+    flat = inds.reshape(-1)
+    owner = np.repeat(np.arange(N), k)
+    # Hub targets with ~60, ~500, ~3,000 and ~9,000 incoming entries.
+    hubs = rng.choice(N, size=34, replace=False)
+    want = [60] * 20 + [500] * 10 + [3000] * 3 + [9000]
+    slots = rng.permutation(flat.size)
+    at = 0
+    for h, m in zip(hubs, want):
+        take = slots[at:at + m]
+        at += m
+        take = take[owner[take] != h]
+        flat[take] = h
+    dists = (rng.integers(0, 8, size=(N, k)) / 8).astype(np.float32)
+    dists = -np.sort(-dists, axis=1)
+    rp, cols, vals = oracle.symmetrize(inds, dists)
+    lens = k + np.bincount(inds.reshape(-1), minlength=N)
+    for lo, hi in [(48, 128), (128, 1024), (1024, 8192), (8192, 1 << 30)]:
+        assert ((lens > lo) & (lens <= hi)).any(), (lo, hi)
     _assert_same(_gpu_sym(cuda, inds, dists), rp, cols, vals)
 
 
