@@ -581,27 +581,97 @@ __device__ __forceinline__ void window_sample(float *win, uint32_t u, Vec<D> &yi
     store_win<D>(win, u, yn);
 }
 
+// The positive sample of edge (i, j) on the held source row yi, with the
+// target row yj (a self edge adds and removes the same step, as the
+// reference's y_i += dx; y_i -= dx on one row, src/ncvis.cpp:337-338).
+template <int D>
+__device__ __forceinline__ void edge_positive(float *Y, uint32_t i, uint32_t j, const Vec<D> &yj,
+                                              const EpochConst &k, float &Qc, Vec<D> &yi) {
+    if (j != i) {
+        const float w = nce_weight(sq_dist<D>(yi, yj), true, k, Qc);
+        Vec<D> dx;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            dx.v[c] = clip4((yj.v[c] - yi.v[c]) * w);
+            yi.v[c] += dx.v[c];
+        }
+        sub_row<D>(Y, j, dx);
+    } else {
+        const float w = nce_weight(0.f, true, k, Qc);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const float dx = clip4(0.f * w);
+            yi.v[c] = (yi.v[c] + dx) - dx;
+        }
+    }
+}
+
+// The nu noise samples of edge e (source i) from the round's window.
+// kMulShift: every pick is a 32-bit Philox word scaled to the window by
+// multiply-shift (four per block; exactly uniform for any window size W, as
+// the window of a whole small problem needs; for a power of two it takes the
+// word's top bits); otherwise eight 16-bit halves of a block masked to the
+// power-of-two window.
+template <int D, bool kMulShift>
+__device__ __forceinline__ void edge_noise(int64_t e, uint32_t i, const EpochConst &k, float &Qc,
+                                           uint32_t key0, uint32_t key1, uint32_t tag, float *win,
+                                           const WindowSpec &ws, Vec<D> &yi) {
+    if constexpr (kMulShift) {
+        for (int s0 = 0; s0 < k.nu; s0 += 4) {
+            const Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), tag,
+                                               (uint32_t)(s0 >> 2) | 0x50000000u, key0, key1);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (s0 + t >= k.nu) break;
+                const uint32_t pick = (uint32_t)(((uint64_t)r.v[t] * ws.W) >> 32);
+                const uint32_t u =
+                    window_redraw(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 + t), pick, i, ws);
+                window_sample<D>(win, u, yi, k, Qc);
+            }
+        }
+    } else {
+        for (int s0 = 0; s0 < k.nu; s0 += 8) {
+            const Philox4x32 r = window_block(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 >> 3));
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                if (s0 + t >= k.nu) break;
+                const uint32_t u = window_redraw(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 + t),
+                                                 window_pick(r, t, ws.W), i, ws);
+                window_sample<D>(win, u, yi, k, Qc);
+            }
+        }
+    }
+}
+
+// Switches the held source row to i (writing the previous one back).
+template <int D>
+__device__ __forceinline__ void hold_source(float *Y, uint32_t i, bool &have, uint32_t &ci,
+                                            Vec<D> &yi, Vec<D> &yi0) {
+    if (!have || i != ci) {
+        if (have) put_row<D>(Y, ci, yi, yi0);
+        ci = i;
+        yi = load_row<D>(Y, ci);
+        yi0 = yi;
+        have = true;
+    }
+}
+
 // Edges [a, b) of a chain against the round's window; the chain's current
 // source row (ci, yi, read as yi0; valid when `have`) carries over rounds and
-// is written back by put_row.
-// The edges run as a software pipeline of depth P: while edge e runs, the
-// positive rows of edges e+1 .. e+P are already in flight and the indices of
-// edge e+P+1 are being read, so a chain waits for a gather only when its edges
-// are shorter than the memory round trip.  A gathered row that this chain may
-// have written between the gather and its use (the source it held at the
-// gather, or the source or target of an edge run in between) is read again,
-// so the chain always sees its own updates.  kMulShift: every pick is a 32-bit
-// Philox word scaled to the window by multiply-shift (four per block; exactly
-// uniform for any window size W, as the window of a whole small problem needs;
-// for a power of two it takes the word's top bits); otherwise eight 16-bit
-// halves of a block masked to the power-of-two window.
+// is written back by put_row.  Two schedules of the positive gathers, both
+// exact for one chain: a gathered row that this chain may have written
+// between the gather and its use is read again, so the chain always sees its
+// own updates.
+//
+// Pipelined (window_edges_pipelined): while edge e runs, the positive rows of
+// edges e+1 .. e+P are in flight and the indices of edge e+P+1 are being
+// read; rows written in between are the source held at the gather and the
+// sources and targets of the edges run in between.
 template <int D, bool kMulShift, int P>
-__device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict__ src,
-                                             const int32_t *__restrict__ dst, int64_t a, int64_t b,
-                                             const EpochConst &k, float &Qc, uint32_t key0,
-                                             uint32_t key1, uint32_t tag, float *win,
-                                             const WindowSpec &ws, bool &have, uint32_t &ci,
-                                             Vec<D> &yi, Vec<D> &yi0) {
+__device__ __forceinline__ void window_edges_pipelined(
+    float *Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst, int64_t a,
+    int64_t b, const EpochConst &k, float &Qc, uint32_t key0, uint32_t key1, uint32_t tag,
+    float *win, const WindowSpec &ws, bool &have, uint32_t &ci, Vec<D> &yi, Vec<D> &yi0) {
     static_assert(P >= 1 && P <= 3, "pipeline depth");
     if (a >= b) return;
     // Slot q holds edge e+q: indices for q <= P, the gathered row and its
@@ -629,59 +699,9 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
         const int32_t nd = e + P + 1 < b ? dst[e + P + 1] : -1;
 
         const uint32_t i = (uint32_t)ps[0], j = (uint32_t)pd[0];
-        if (!have || i != ci) {
-            if (have) put_row<D>(Y, ci, yi, yi0);
-            ci = i;
-            yi = load_row<D>(Y, ci);
-            yi0 = yi;
-            have = true;
-        }
-        if (j != i) {
-            const Vec<D> yjv = pst[0] ? load_row<D>(Y, j) : pyj[0];
-            const float w = nce_weight(sq_dist<D>(yi, yjv), true, k, Qc);
-            Vec<D> dx;
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                dx.v[c] = clip4((yjv.v[c] - yi.v[c]) * w);
-                yi.v[c] += dx.v[c];
-            }
-            sub_row<D>(Y, j, dx);
-        } else {
-            // A self edge: y_i += dx then y_i -= dx on one row (src/ncvis.cpp:337-338).
-            const float w = nce_weight(0.f, true, k, Qc);
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const float dx = clip4(0.f * w);
-                yi.v[c] = (yi.v[c] + dx) - dx;
-            }
-        }
-        if constexpr (kMulShift) {
-            // The four 32-bit words of a Philox block give four picks by
-            // multiply-shift.
-            for (int s0 = 0; s0 < k.nu; s0 += 4) {
-                const Philox4x32 r = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), tag,
-                                                   (uint32_t)(s0 >> 2) | 0x50000000u, key0, key1);
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    if (s0 + t >= k.nu) break;
-                    const uint32_t pick = (uint32_t)(((uint64_t)r.v[t] * ws.W) >> 32);
-                    const uint32_t u =
-                        window_redraw(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 + t), pick, i, ws);
-                    window_sample<D>(win, u, yi, k, Qc);
-                }
-            }
-        } else {
-            for (int s0 = 0; s0 < k.nu; s0 += 8) {
-                const Philox4x32 r = window_block(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 >> 3));
-#pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    if (s0 + t >= k.nu) break;
-                    const uint32_t u = window_redraw(key0, key1, (uint64_t)e, tag, (uint32_t)(s0 + t),
-                                                     window_pick(r, t, ws.W), i, ws);
-                    window_sample<D>(win, u, yi, k, Qc);
-                }
-            }
-        }
+        hold_source<D>(Y, i, have, ci, yi, yi0);
+        edge_positive<D>(Y, i, j, (j != i && pst[0]) ? load_row<D>(Y, j) : pyj[0], k, Qc, yi);
+        edge_noise<D, kMulShift>(e, i, k, Qc, key0, key1, tag, win, ws, yi);
         // Rows in flight that edge e may have written: its source (stored at
         // a later switch), its target, and for the row gathered at this edge
         // the source held before it.
@@ -697,12 +717,71 @@ __device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict
     }
 }
 
-// Depth of the edge pipeline: one edge ahead (37.3 ms for the 1,024,000-point
-// optimizer against 41.1 ms for the positive rows of four edges gathered
-// together); two and three edges ahead measured 37.4 and 39.2 ms.
-constexpr int kEdgePipeline = 1;
+// Grouped (window_edges_grouped): the indices of four edges in one vector load
+// each and their positive rows gathered together before the group runs; rows
+// written in between are the source held at the gather and the group's
+// earlier sources and targets.  (a is a multiple of 4.)
+template <int D, bool kMulShift>
+__device__ __forceinline__ void window_edges_grouped(
+    float *Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst, int64_t a,
+    int64_t b, const EpochConst &k, float &Qc, uint32_t key0, uint32_t key1, uint32_t tag,
+    float *win, const WindowSpec &ws, bool &have, uint32_t &ci, Vec<D> &yi, Vec<D> &yi0) {
+    for (int64_t e = a; e < b; e += 4) {
+        int32_t sv[4], dv[4];
+        if (e + 4 <= b && (e & 3) == 0) {
+            const int4 s4 = __ldg(reinterpret_cast<const int4 *>(src + e));
+            const int4 d4 = __ldg(reinterpret_cast<const int4 *>(dst + e));
+            sv[0] = s4.x, sv[1] = s4.y, sv[2] = s4.z, sv[3] = s4.w;
+            dv[0] = d4.x, dv[1] = d4.y, dv[2] = d4.z, dv[3] = d4.w;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                sv[q] = e + q < b ? src[e + q] : -1;
+                dv[q] = e + q < b ? dst[e + q] : -1;
+            }
+        }
+        Vec<D> yj[4] = {};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (dv[q] >= 0 && dv[q] != sv[q]) yj[q] = load_row<D>(Y, dv[q]);
+        const int32_t ci0 = have ? (int32_t)ci : -1;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (e + q >= b) break;
+            const uint32_t i = (uint32_t)sv[q], j = (uint32_t)dv[q];
+            hold_source<D>(Y, i, have, ci, yi, yi0);
+            bool stale = dv[q] == ci0;
+#pragma unroll
+            for (int x = 0; x < q; ++x) stale |= (dv[q] == sv[x]) | (dv[q] == dv[x]);
+            edge_positive<D>(Y, i, j, (j != i && stale) ? load_row<D>(Y, j) : yj[q], k, Qc, yi);
+            edge_noise<D, kMulShift>(e + q, i, k, Qc, key0, key1, tag, win, ws, yi);
+        }
+    }
+}
 
-template <int D>
+// Schedule by the epoch's noise count: with one noise sample per edge an edge
+// is too short for a one-edge pipeline to cover a gather, and the grouped
+// form is faster (1,024,000 points, ms per epoch at nu = 1 / 2 / 4 / 8 / 16:
+// grouped 0.497 / 0.580 / 0.734 / 1.03 / 1.67, pipelined one edge ahead 0.540
+// / 0.568 / 0.653 / 0.860 / 1.39; two and three edges ahead were slower).
+// Each kernel instance carries one of them (kGrouped); the single-problem
+// optimizer takes the grouped one in the epochs with nu = 1.
+template <int D, bool kMulShift, bool kGrouped>
+__device__ __forceinline__ void window_edges(float *Y, const int32_t *__restrict__ src,
+                                             const int32_t *__restrict__ dst, int64_t a, int64_t b,
+                                             const EpochConst &k, float &Qc, uint32_t key0,
+                                             uint32_t key1, uint32_t tag, float *win,
+                                             const WindowSpec &ws, bool &have, uint32_t &ci,
+                                             Vec<D> &yi, Vec<D> &yi0) {
+    if constexpr (kGrouped)
+        window_edges_grouped<D, kMulShift>(Y, src, dst, a, b, k, Qc, key0, key1, tag, win, ws,
+                                           have, ci, yi, yi0);
+    else
+        window_edges_pipelined<D, kMulShift, 1>(Y, src, dst, a, b, k, Qc, key0, key1, tag, win,
+                                                ws, have, ci, yi, yi0);
+}
+
+template <int D, bool kGrouped>
 __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
     float *__restrict__ Y, const int32_t *__restrict__ src, const int32_t *__restrict__ dst,
     int64_t E, uint32_t N, const float *__restrict__ Q_in, double *__restrict__ q_part,
@@ -736,8 +815,8 @@ __global__ void __launch_bounds__(kWinThreads, 2) sgd_epoch_window(
         const int64_t a = min(e1, e0 + (int64_t)r * round_edges);
         const int64_t b = min(e1, a + round_edges);
         const WindowSpec ws{seg, W, N, 0u, false};
-        window_edges<D, false, kEdgePipeline>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws,
-                               have, ci, yi, yi0);
+        window_edges<D, false, kGrouped>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch,
+                                         win, ws, have, ci, yi, yi0);
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < W; u += kWinThreads) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
@@ -821,8 +900,10 @@ __global__ void __launch_bounds__(T) sgd_epoch_window_batched(
         // One pick scheme for both window forms, so the kernel carries one copy
         // of the edge loop (with two, its blocks of both forms on one SM
         // thrashed the instruction cache).
-        window_edges<D, true, kEdgePipeline>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win, ws, have,
-                              ci, yi, yi0);
+        // The pipelined schedule in every epoch (the grouped one measured the
+        // same at one noise sample per edge on the 256-problem workload).
+        window_edges<D, true, false>(Y, src, dst, a, b, k, Qc, key0, key1, (uint32_t)epoch, win,
+                                     ws, have, ci, yi, yi0);
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < W; u += T) {
             const Vec<D> now = load_win<D>(win, u), was = load_win<D>(loaded, u);
@@ -1045,11 +1126,16 @@ template <int D>
 void launch_window_epoch(unsigned blocks, size_t smem, cudaStream_t s, const SgdArgs &g,
                          double *q_part, const EpochConst &k, int ep, uint32_t key0, uint32_t key1,
                          int64_t chunk, int64_t chains, uint32_t W, int round_edges) {
-    NCVIS_CUDA(cudaFuncSetAttribute(sgd_epoch_window<D>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    NCVIS_LAUNCH(sgd_epoch_window<D>, blocks, kWinThreads, smem, s, g.Y, g.src, g.dst,
-                 g.E, (uint32_t)g.N, g.Q, q_part, k, ep, key0, key1, chunk, chains, W,
-                 round_edges);
+    auto launch = [&](auto kernel) {
+        NCVIS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        NCVIS_LAUNCH(kernel, blocks, kWinThreads, smem, s, g.Y, g.src, g.dst, g.E, (uint32_t)g.N,
+                     g.Q, q_part, k, ep, key0, key1, chunk, chains, W, round_edges);
+    };
+    if (k.nu == 1)
+        launch(sgd_epoch_window<D, true>);
+    else
+        launch(sgd_epoch_window<D, false>);
 }
 
 int64_t window_resident_chains(int d) {
@@ -1061,10 +1147,10 @@ int64_t window_resident_chains(int d) {
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kWinThreads, smem);
     };
     switch (d) {
-        case 1: err = occ(sgd_epoch_window<1>); break;
-        case 2: err = occ(sgd_epoch_window<2>); break;
-        case 3: err = occ(sgd_epoch_window<3>); break;
-        default: err = occ(sgd_epoch_window<4>);
+        case 1: err = occ(sgd_epoch_window<1, false>); break;
+        case 2: err = occ(sgd_epoch_window<2, false>); break;
+        case 3: err = occ(sgd_epoch_window<3, false>); break;
+        default: err = occ(sgd_epoch_window<4, false>);
     }
     if (err != cudaSuccess || blocks < 1) blocks = 1;
     return (int64_t)blocks * kWinThreads * num_sms();
