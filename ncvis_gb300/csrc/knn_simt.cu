@@ -261,7 +261,10 @@ __global__ void __launch_bounds__(128) rerank_rows(const float *__restrict__ Xp,
             qv[t] = c < D ? q[c] : 0.f;
         }
     }
-    constexpr int U = 4;  // candidates in flight per warp
+    // Candidates in flight per warp: 8 (64 registers) took the rerank of
+    // 1,024,000 rows x 32 candidates from 3.84 to 2.68 ms against 4; 16 (128
+    // registers, half the resident warps) 4.02 ms.
+    constexpr int U = 8;
     for (int c0 = 0; c0 < C; c0 += U) {
         int idx[U];
         float part[U];
