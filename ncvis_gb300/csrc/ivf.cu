@@ -135,12 +135,35 @@ __global__ void ivf_accumulate_shared(const float *__restrict__ Xp, int64_t N, i
     for (int t = threadIdx.x; t < C; t += blockDim.x) scnt[t] = 0;
     __syncthreads();
     const int warps = blockDim.x >> 5, lane = threadIdx.x & 31;
-    for (int64_t i = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5); i < N;
-         i += (int64_t)gridDim.x * warps) {
-        const int c = cand[i * R];
-        if (c < 0 || c >= C) continue;
-        for (int t = lane; t < D; t += 32) atomicAdd(ssum + c * D + t, Xp[i * D + t]);
-        if (lane == 0) atomicAdd(scnt + c, 1);
+    // Rows of up to 128 columns: each lane's four values of the next row are
+    // loaded while the current row's are added (the cell ordering of
+    // 1,024,000 x 100: 4.55 -> 3.26 ms over its three passes).
+    const int64_t step = (int64_t)gridDim.x * warps;
+    int64_t i = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+    float v[4];
+    int c = -1;
+    auto load = [&](int64_t r) {
+        c = r < N ? cand[r * R] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int t = lane + 32 * u;
+            v[u] = (r < N && t < D) ? Xp[r * D + t] : 0.f;
+        }
+    };
+    load(i);
+    for (; i < N; i += step) {
+        const int cc = c;
+        float w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) w[u] = v[u];
+        load(i + step);
+        if (cc < 0 || cc >= C) continue;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int t = lane + 32 * u;
+            if (t < D) atomicAdd(ssum + cc * D + t, w[u]);
+        }
+        if (lane == 0) atomicAdd(scnt + cc, 1);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < C * D; t += blockDim.x)
@@ -296,7 +319,7 @@ void kmeans_cells(const float *Xp, const __nv_bfloat16 *Xb, int64_t N, int D,
     // Per-block sums in shared memory where C * D floats fit in 110 KB (two
     // blocks per SM), else straight into the global sums.
     const size_t acc_smem = sizeof(float) * (size_t)C * D + sizeof(int) * (size_t)C;
-    const bool shared_acc = acc_smem <= 110 * 1024;
+    const bool shared_acc = acc_smem <= 110 * 1024 && D <= 128;  // four values per lane
     if (shared_acc)
         NCVIS_CUDA(cudaFuncSetAttribute(ivf_accumulate_shared,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
