@@ -19,9 +19,10 @@
 //      (distance, position) items, runs the libstdc++-equivalent introsort
 //      (introsort.cuh) and the in-place deduplication, all in the thread's
 //      slots of shared memory (merge_rows_thread, rows of up to 48 items);
-//      longer rows are listed and merged one warp per row (merge_rows_warp,
-//      tiers of 128, 1,024 and 8,192 items), longer still on a row-aligned
-//      global scratch;
+//      longer rows are listed and merged one warp per row (merge_rows_wpar up
+//      to 128 items, the sort spread over the lanes; merge_rows_warp in tiers
+//      of 1,024 and 8,192 items), longer still on a row-aligned global
+//      scratch;
 //   4. scan of the kept counts -> row_ptr; compact_rows writes cols, vals and
 //      the source row of every entry (the build_edges pairs).
 #include <algorithm>
@@ -37,12 +38,14 @@ namespace {
 
 // Merge tiers by row length k + in-degree (~30 on average): up to 48 items
 // one thread per row (12 B per item in shared memory: the sort item and the
-// row's index at that position; 3 blocks of 128 threads per SM); longer rows
-// one warp per row, in tiers of 128, 1,024 and 8,192 items (hubs: rows of up
-// to ~1,000 items occur in 64-dimensional mixtures of a few thousand points);
-// longer still on the global scratch.
+// row's index at that position; 3 blocks of 128 threads per SM); up to 128
+// items one warp per row with the sort spread over the lanes
+// (merge_rows_wpar); longer rows one warp per row with the sort on one lane,
+// in tiers of 1,024 and 8,192 items (hubs: rows of up to ~1,000 items occur in
+// 64-dimensional mixtures of a few thousand points); longer still on the
+// global scratch.
 constexpr int kCap0 = 48, kThreads0 = 128;
-constexpr int kCap1 = 128, kWarps1 = 8;
+constexpr int kWarps1 = 8;
 constexpr int kCap2 = 1024, kWarps2 = 4;
 constexpr int kCap3 = 8192, kWarps3 = 1;
 
@@ -232,11 +235,258 @@ __global__ void __launch_bounds__(32 * W, 1) merge_rows_warp(
     }
 }
 
+// Data-parallel warp tier: rows of up to 128 items, one warp each, with the
+// sort and the deduplication spread over the lanes and results identical to
+// the sequential ones:
+//   * each Hoare partition of the introsort (median of three into the first
+//     slot by lane 0) is computed from two position lists built by ballots:
+//     G, the positions after the pivot whose key is not below it, ascending;
+//     S, the positions whose key is not above it, descending, with the
+//     pivot's own position last.  The t-th swap exchanges G[t] and S[t] for
+//     every t with G[t] < S[t]; after t* swaps the cut is
+//     min(G[t*], S[t*-1]) (S[-1] = the range's end);
+//   * ranges left at 16 items or fewer, and ranges heap-sorted by lane 0
+//     when the depth budget runs out, are leaves; std::sort's final insertion
+//     sort is stable, so each leaf is then stably sorted by key in place
+//     (every item's rank within its leaf);
+//   * the deduplication's keep flags are the fixpoint of one parallel step
+//     (item j kept or not from the kept items of the previous guess), which
+//     agrees with the sequential loop from the start up to one more item per
+//     step.
+// Shared memory per warp: WparRow.
+constexpr int kWparCap = 128;
+struct WparRow {
+    SortItem items[kWparCap];
+    int32_t orig[kWparCap];
+    int32_t ids[kWparCap];
+    int16_t G[kWparCap], S[kWparCap], kl[kWparCap];
+    uint8_t blo[kWparCap], bhi_m1[kWparCap];  // leaf [blo, bhi_m1 + 1)
+};
+
+__device__ __forceinline__ int32_t warp_partition(WparRow &w, int32_t lo, int32_t hi, int lane) {
+    if (lane == 0)
+        introsort_detail::median_to(w.items, lo, lo + 1, lo + (hi - lo) / 2, hi - 1);
+    __syncwarp();
+    const float P = w.items[lo].key;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned bg[4], bl[4];
+    int nl = 1;  // the pivot's own position
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int32_t p = lo + 1 + 32 * m + lane;
+        const bool valid = p < hi;
+        const float key = valid ? w.items[p].key : 0.f;
+        bg[m] = __ballot_sync(0xffffffffu, valid && !(key < P));
+        bl[m] = __ballot_sync(0xffffffffu, valid && !(P < key));
+        nl += __popc(bl[m]);
+    }
+    int ng = 0, cl = 0;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int32_t p = lo + 1 + 32 * m + lane;
+        if ((bg[m] >> lane) & 1u) w.G[ng + __popc(bg[m] & lt)] = (int16_t)p;
+        if ((bl[m] >> lane) & 1u) w.S[nl - 2 - cl - __popc(bl[m] & lt)] = (int16_t)p;
+        ng += __popc(bg[m]);
+        cl += __popc(bl[m]);
+    }
+    if (lane == 0) w.S[nl - 1] = (int16_t)lo;
+    __syncwarp();
+    const int pairs = min(ng, nl);
+    int ts = 0;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int t = 32 * m + lane;
+        ts += __popc(__ballot_sync(0xffffffffu, t < pairs && w.G[t] < w.S[t]));
+    }
+    // At most 64 swaps (each moves two distinct positions of <= 127).
+    SortItem a[2], b[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int t = 32 * m + lane;
+        if (t < ts) a[m] = w.items[w.G[t]], b[m] = w.items[w.S[t]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int t = 32 * m + lane;
+        if (t < ts) w.items[w.G[t]] = b[m], w.items[w.S[t]] = a[m];
+    }
+    int32_t cut = ts > 0 ? (int32_t)w.S[ts - 1] : hi;
+    if (ts < ng) cut = min(cut, (int32_t)w.G[ts]);
+    __syncwarp();
+    return cut;
+}
+
+template <int W>
+__global__ void __launch_bounds__(32 * W, 1) merge_rows_wpar(
+    int k, const int32_t *__restrict__ inds, const float *__restrict__ dists,
+    const int64_t *__restrict__ in_off, const int32_t *__restrict__ in_key,
+    int32_t *__restrict__ out_col, float *__restrict__ out_val, int32_t *__restrict__ kept,
+    const int32_t *__restrict__ rows, const int32_t *__restrict__ n_rows, int32_t *__restrict__ next,
+    int32_t *__restrict__ n_next) {
+    extern __shared__ __align__(16) unsigned char wpar_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WparRow &w = reinterpret_cast<WparRow *>(wpar_raw)[warp];
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t count = *n_rows;
+    for (int64_t r = (int64_t)blockIdx.x * W + warp; r < count; r += (int64_t)gridDim.x * W) {
+        const int64_t i = rows[r];
+        const int64_t ib = in_off[i];
+        const int nin = (int)(in_off[i + 1] - ib);
+        const int L = k + nin;
+        const int64_t base = i * k + ib;  // row-aligned output offset
+        if (L > kWparCap) {
+            if (lane == 0) next[atomicAdd(n_next, 1)] = (int32_t)i;
+            continue;
+        }
+        // The incoming ids, ranked (distinct), then the row's items.
+        for (int q = lane; q < nin; q += 32) w.orig[k + q] = in_key[ib + q];
+        __syncwarp();
+        for (int q = lane; q < nin; q += 32) {
+            const int32_t e = w.orig[k + q];
+            int rk = 0;
+            for (int t = 0; t < nin; ++t) rk += w.orig[k + t] < e;
+            w.ids[rk] = e;
+        }
+        __syncwarp();
+        for (int p = lane; p < L; p += 32) {
+            if (p < k) {
+                w.items[p] = SortItem{dists[i * k + p], p};
+                w.orig[p] = inds[i * k + p];
+            } else {
+                const int32_t e = w.ids[p - k];
+                w.items[p] = SortItem{dists[e], p};
+                w.orig[p] = e / k;
+            }
+        }
+        __syncwarp();
+        // The introsort's partitions and leaves (a warp-uniform range stack).
+        int32_t st_lo[16], st_hi[16], st_d[16];
+        int top = 0;
+        st_lo[0] = 0, st_hi[0] = L, st_d[0] = 2 * introsort_detail::floor_log2(max(L, 1));
+        top = 1;
+        while (top > 0) {
+            --top;
+            int32_t lo = st_lo[top], hi = st_hi[top], depth = st_d[top];
+            while (hi - lo > 16) {
+                if (depth == 0) {
+                    if (lane == 0)
+                        introsort_detail::heap_sort(
+                            introsort_detail::Offset<SortItem *>{w.items, lo}, hi - lo);
+                    __syncwarp();
+                    break;
+                }
+                --depth;
+                const int32_t cut = warp_partition(w, lo, hi, lane);
+                st_lo[top] = cut, st_hi[top] = hi, st_d[top] = depth;
+                ++top;
+                hi = cut;
+            }
+            for (int32_t x = lo + lane; x < hi; x += 32)
+                w.blo[x] = (uint8_t)lo, w.bhi_m1[x] = (uint8_t)(hi - 1);
+        }
+        __syncwarp();
+        // Each leaf stably sorted by key in place.
+        {
+            SortItem mine[4];
+            int dest[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int x = lane + 32 * m;
+                if (x < L) {
+                    const SortItem it = w.items[x];
+                    const int b0 = w.blo[x], b1 = (int)w.bhi_m1[x] + 1;
+                    int rk = 0;
+                    for (int y = b0; y < b1; ++y) {
+                        const float ky = w.items[y].key;
+                        rk += (ky < it.key) | ((ky == it.key) & (y < x));
+                    }
+                    mine[m] = it;
+                    dest[m] = b0 + rk;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+                if (lane + 32 * m < L) w.items[dest[m]] = mine[m];
+            __syncwarp();
+        }
+        // Deduplication: keep flags to their fixpoint (at most L + 1 steps).
+        unsigned K[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) K[m] = __ballot_sync(0xffffffffu, lane + 32 * m < L);
+        for (int step = 0; step <= L + 1; ++step) {
+            int nj[4], before = 0;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                nj[m] = before + __popc(K[m] & lt);
+                if ((K[m] >> lane) & 1u) w.kl[nj[m]] = (int16_t)(lane + 32 * m);
+                before += __popc(K[m]);
+            }
+            __syncwarp();
+            bool same = true;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int j = lane + 32 * m;
+                bool kp = false;
+                if (j < L) {
+                    if (j == 0) {
+                        kp = true;
+                    } else {
+                        const int p = w.items[j].pos, q = w.items[j - 1].pos, n = nj[m];
+                        const int32_t vp = w.orig[p < n ? w.items[w.kl[p]].pos : p];
+                        const int32_t vq = w.orig[q < n ? w.items[w.kl[q]].pos : q];
+                        kp = vp != vq;
+                    }
+                }
+                const unsigned nk = __ballot_sync(0xffffffffu, kp);
+                same &= nk == K[m];
+                K[m] = nk;
+            }
+            if (same) break;
+            __syncwarp();
+        }
+        int n_out = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) n_out += __popc(K[m]);
+        for (int q = lane; q < n_out; q += 32) {
+            const SortItem it = w.items[w.kl[q]];
+            out_col[base + q] = w.orig[it.pos];
+            out_val[base + q] = it.key;
+        }
+        if (lane == 0) kept[i] = n_out;
+        __syncwarp();
+    }
+}
+
+template <int W>
+void launch_merge_wpar(int k, const int32_t *inds, const float *dists, const int64_t *in_off,
+                       int32_t *in_key, int32_t *out_col, float *out_val, int32_t *kept,
+                       const int32_t *rows, const int32_t *n_rows, int32_t *next, int32_t *n_next,
+                       cudaStream_t s);
+
 // Blocks per SM for a block of `threads` threads and `smem` bytes of shared
 // memory (the warp tiers use 64 registers per thread: 1,024 threads per SM).
 inline int blocks_per_sm(size_t smem, int threads) {
     const int by_smem = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
     return std::max(1, std::min(by_smem, 1024 / threads));
+}
+
+template <int W>
+void launch_merge_wpar(int k, const int32_t *inds, const float *dists, const int64_t *in_off,
+                       int32_t *in_key, int32_t *out_col, float *out_val, int32_t *kept,
+                       const int32_t *rows, const int32_t *n_rows, int32_t *next, int32_t *n_next,
+                       cudaStream_t s) {
+    const size_t smem = sizeof(WparRow) * W;
+    NCVIS_CUDA(cudaFuncSetAttribute(merge_rows_wpar<W>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // A grid of resident blocks (registers, not shared memory, bound them).
+    int per_sm = 0;
+    NCVIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, merge_rows_wpar<W>, 32 * W,
+                                                             smem));
+    const int64_t grid = (int64_t)num_sms() * std::max(per_sm, 1);
+    NCVIS_LAUNCH((merge_rows_wpar<W>), grid, 32 * W, smem, s, k, inds, dists, in_off, in_key,
+                 out_col, out_val, kept, rows, n_rows, next, n_next);
 }
 
 template <int C, int W>
@@ -361,9 +611,8 @@ int64_t run_symmetrize(int64_t N, int k, const int32_t *inds, const float *dists
                      smem, s, N, k, inds, dists, w.in_off, w.in_key, w.out_col, w.out_val, w.kept,
                      w.tier1, w.n_tier);
     }
-    launch_merge_warp<kCap1, kWarps1>(k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
-                                      w.out_val, w.kept, w.tier1, w.n_tier, w.tier2, w.n_tier + 1,
-                                      s);
+    launch_merge_wpar<kWarps1>(k, inds, dists, w.in_off, w.in_key, w.out_col, w.out_val, w.kept,
+                               w.tier1, w.n_tier, w.tier2, w.n_tier + 1, s);
     launch_merge_warp<kCap2, kWarps2>(k, inds, dists, w.in_off, w.in_key, w.items, w.out_col,
                                       w.out_val, w.kept, w.tier2, w.n_tier + 1, w.tier1,
                                       w.n_tier + 2, s);

@@ -40,3 +40,22 @@ def test_staged_row_merge_matches_reference_steps(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok "), r.stdout
     assert int(r.stdout.split()[1]) >= 20000
+
+
+def test_data_parallel_row_sort_matches_std_sort(tmp_path):
+    """The data-parallel restatement behind the GPU's warp-per-row merge:
+    std::sort's Hoare partitions computed from position lists, each leaf
+    range stably sorted, and the in-place deduplication as a fixpoint of one
+    parallel step, against std::sort with the reference's comparator and the
+    sequential merge (src/knntable.cpp:81-93), on random, tie-heavy and
+    adversarial rows that exhaust the depth budget
+    (tests/harness/partition_check.cpp)."""
+    src = os.path.join(ROOT, "tests", "harness", "partition_check.cpp")
+    exe = str(tmp_path / "partition_check")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "ncvis_gb300", "csrc"),
+                        src, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe, "20000"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok "), r.stdout
+    assert int(r.stdout.split()[1]) >= 20000
