@@ -27,14 +27,6 @@ namespace {
 
 constexpr int kThreads = kNceThreads;
 
-__device__ __forceinline__ float softplus(float u) {
-    return fmaxf(u, 0.f) + log1pf(__expf(-fabsf(u)));
-}
-
-__device__ __forceinline__ float sigmoid(float u) {
-    return u >= 0.f ? 1.f / (1.f + __expf(-u)) : __expf(u) / (1.f + __expf(u));
-}
-
 struct NceConst {
     float a, b, log_nu, Q, pow_b1_at_zero;
     int nu;
